@@ -1,0 +1,355 @@
+#!/usr/bin/env python
+"""Benchmark of the alignment path on GB300: alignments/s on the short-read
+workload (1,000,000 pairs of 150 bases, per-position edit probability 0.05,
+batches of 100,000 pairs, synthetic data from a fixed seed).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step aligns one batch of 100,000 pairs: distances and full CIGARs.
+  value  device-resident throughput: the batch's ASCII and descriptors are
+         already in HBM, results stay in HBM; timed with CUDA events on the
+         launching stream.  Steps cycle over the 10 batches of the workload
+         (300 MB of ASCII + 152 MB of CIGAR slots > the 129 MB L2).
+  e2e    the same workload through the host-buffer C call wfe_align with
+         pinned host buffers: host->device copies of every batch's inputs and
+         device->host copies of its distances, status and CIGARs are inside
+         the timed region.
+--impl reference times the CPU restatement of the reference's algorithm
+(oracle/, the reference has no CPU aligner of its own and its sources are
+not on this machine) on every host core.
+
+One process per GPU (torchrun for N > 1): every rank aligns its own
+1,000,000-pair shard (weak scaling, no collective on the data path); rank 0
+prints one JSON line with the max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "ewfa-gpu_gb300"))
+
+import numpy as np  # noqa: E402
+
+import wfe  # noqa: E402
+
+PAIRS, BATCH, LENGTH, EDIT_P, SEED = 1_000_000, 100_000, 150, 0.05, 2
+METRIC = "alignments/sec"
+WORKLOAD = (f"short reads: {PAIRS:,} pairs x {LENGTH} bases, edit probability {EDIT_P}, "
+            f"batches of {BATCH:,}; distance + full CIGAR per pair")
+CIGAR_STRIDE = wfe.reference_cigar_stride(LENGTH)   # the reference's cigar_max_len for -l 150
+MAX_SEQ_LEN = 2 * LENGTH                             # the reference reader's slot holds 2*l bases
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def reduce_max(x: float, world: int, device=None) -> float:
+    """Max of x over ranks (identity for one process)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int, device=None) -> None:
+    if world > 1:
+        import torch.distributed as dist
+        if device is not None:
+            dist.barrier(device_ids=[device.index])
+        else:
+            dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        mhz = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[j] for r in rows for j in range(4) if r[5 + j].lower() == "active"})
+        return {"sm_mhz": statistics.median(mhz) if mhz else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary, if one records it (a line 'traffic_bytes_per_launch: N')."""
+    p = os.path.join(ROOT, "profiles", "tier0_short_reads.txt")
+    try:
+        for line in open(p):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def cigar_lengths(cg: np.ndarray) -> np.ndarray:
+    """Bytes of each encoded CIGAR before its terminator."""
+    z = cg == 0
+    has = z.any(1)
+    return np.where(has, z.argmax(1), cg.shape[1])
+
+
+def cpu_baseline(ascii, pairs, nthreads):
+    """The CPU restatement of the reference (oracle/) on all host cores, on
+    the whole workload (about 1-2 s of CPU time per 1M pairs and core)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build(ref=False)
+    t0 = time.perf_counter()
+    oracle.align_batch(ascii, pairs["p_off"], pairs["p_len"], pairs["t_off"], pairs["t_len"], CIGAR_STRIDE,
+                       nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    return {"value": len(pairs) / dt, "unit": METRIC, "cores": nthreads, "kind": "port",
+            "sample": f"all {len(pairs):,} pairs of the workload, {nthreads} threads, {dt:.2f} s"}
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    ascii, pairs = wfe.generate(PAIRS, LENGTH, p_min=EDIT_P, seed=SEED)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build(ref=False)
+    nthreads = os.cpu_count() or 1
+    nb = PAIRS // BATCH
+
+    def step(i):
+        sl = pairs[(i % nb) * BATCH:(i % nb + 1) * BATCH]
+        oracle.align_batch(ascii, sl["p_off"], sl["p_len"], sl["t_off"], sl["t_len"], CIGAR_STRIDE,
+                           nthreads=nthreads)
+
+    for i in range(args.warmup):
+        step(i)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        step(i)
+    dt = time.perf_counter() - t0
+    value = args.steps * BATCH / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "alignments/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded generator)",
+        "config": {"workload": WORKLOAD, "pairs": PAIRS, "batch": BATCH, "length": LENGTH, "edit_prob": EDIT_P,
+                   "seed": SEED},
+        "cpu_baseline": {"value": value, "unit": "alignments/s", "cores": nthreads, "kind": "port",
+                         "sample": f"{args.steps} batches of {BATCH:,} pairs, {nthreads} threads; the CPU "
+                                   "restatement of the reference's kernels (the reference has no CPU aligner)"},
+        "e2e": {"value": value, "unit": "alignments/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    world, rank, local = dist_env()
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA device")
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=device)
+
+    # this rank's shard of the workload
+    ascii, pairs = wfe.generate(PAIRS, LENGTH, p_min=EDIT_P, seed=SEED + 1000 * rank)
+    nb = PAIRS // BATCH
+    stream = torch.cuda.Stream(device=device)
+
+    # ---------------- value: inputs resident in HBM --------------------------
+    d_ascii = torch.from_numpy(ascii).to(device)
+    d_pairs = torch.from_numpy(pairs.view(np.uint8)).to(device)
+    d_dist = torch.zeros(PAIRS, dtype=torch.int32, device=device)
+    d_cigar = torch.zeros(PAIRS * CIGAR_STRIDE, dtype=torch.int8, device=device)
+    d_status = torch.zeros(PAIRS, dtype=torch.uint8, device=device)
+    ctx = wfe.Context(max_seq_len=MAX_SEQ_LEN, batch_size=BATCH, cigar_stride=CIGAR_STRIDE, device=local,
+                      flags=wfe.FLAG_KERNEL_TIMING)
+    pair_bytes = wfe.PAIR_DTYPE.itemsize
+
+    def step(i):
+        b = i % nb
+        ctx.align_device(d_ascii, d_pairs.data_ptr() + b * BATCH * pair_bytes, BATCH, MAX_SEQ_LEN,
+                         d_dist.data_ptr() + 4 * b * BATCH, d_cigar.data_ptr() + b * BATCH * CIGAR_STRIDE,
+                         d_status.data_ptr() + b * BATCH, stream)
+
+    with torch.cuda.stream(stream):
+        for i in range(max(3, args.warmup)):
+            step(i)
+    torch.cuda.synchronize()
+    ctx.reset_stats()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(world, device)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        start.record(stream)
+        for i in range(args.steps):
+            step(i)
+        end.record(stream)
+        torch.cuda.synchronize()
+    barrier(world, device)
+    ms = start.elapsed_time(end)
+    ms_max = reduce_max(ms, world, device)
+    st = ctx.stats()
+    value = world * args.steps * BATCH / (ms_max / 1e3)
+
+    # algorithmic bytes of one batch: ASCII read once, descriptors, and the
+    # distance, status and CIGAR bytes (with terminator) written
+    cg = d_cigar.view(PAIRS, CIGAR_STRIDE).cpu().numpy()
+    st_h = d_status.cpu().numpy()
+    assert (st_h == 0).all(), "non-OK pair status in the benchmark workload"
+    clen = np.minimum(cigar_lengths(cg) + 1, CIGAR_STRIDE)
+    bytes_per_batch = []
+    for b in range(nb):
+        sl = slice(b * BATCH, (b + 1) * BATCH)
+        bytes_per_batch.append(int(pairs["p_len"][sl].sum() + pairs["t_len"][sl].sum()) +
+                               BATCH * (pair_bytes + 4 + 1) + int(clen[sl].sum()))
+    alg_bytes = float(np.mean([bytes_per_batch[i % nb] for i in range(args.steps)]))
+    tier_ms = st["tier_ms"]
+    top = int(np.argmax(tier_ms))
+    launch_ms = tier_ms[top] / max(1, st["tier_launches"][top])
+    peak, peak_kind = measured_hbm_peak()
+    achieved = alg_bytes / (launch_ms / 1e3) / 1e9
+    traffic = profiled_traffic()
+    gpu_launches = int(st["kernel_launches"])
+
+    # ---------------- e2e: host buffers through wfe_align ---------------------
+    h_ascii = torch.empty(len(ascii), dtype=torch.uint8, pin_memory=True).numpy()
+    h_ascii[:] = ascii
+    h_pairs = torch.empty(PAIRS * pair_bytes, dtype=torch.uint8, pin_memory=True).numpy().view(wfe.PAIR_DTYPE)
+    h_pairs[:] = pairs
+    h_dist = torch.empty(PAIRS, dtype=torch.int32, pin_memory=True).numpy()
+    h_cigar = torch.empty(PAIRS * CIGAR_STRIDE, dtype=torch.int8, pin_memory=True).numpy().reshape(PAIRS, CIGAR_STRIDE)
+    h_status = torch.empty(PAIRS, dtype=torch.uint8, pin_memory=True).numpy()
+    ctx2 = wfe.Context(max_seq_len=MAX_SEQ_LEN, batch_size=BATCH, cigar_stride=CIGAR_STRIDE, device=local)
+    ctx2.align(h_ascii, h_pairs, out=(h_dist, h_cigar, h_status))  # warm-up
+    reps = max(1, args.steps // nb)
+    ctx2.reset_stats()
+    barrier(world, device)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        ctx2.align(h_ascii, h_pairs, out=(h_dist, h_cigar, h_status))
+    torch.cuda.synchronize()
+    e2e_s = reduce_max(time.perf_counter() - t0, world, device)
+    barrier(world, device)
+    st2 = ctx2.stats()
+    e2e = {"value": world * reps * PAIRS / e2e_s, "unit": "alignments/s",
+           "h2d_bytes_per_step": int(st2["h2d_bytes"] // max(1, st2["batches"])),
+           "d2h_bytes_per_step": int(st2["d2h_bytes"] // max(1, st2["batches"])),
+           "steps": reps * nb}
+    if not (np.array_equal(h_dist, d_dist.cpu().numpy())):
+        raise SystemExit("host-buffer and device-buffer results differ")
+
+    base = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        base = cpu_baseline(ascii, pairs, os.cpu_count() or 1)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "alignments/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded generator; no dataset)",
+            "config": {"workload": WORKLOAD, "pairs_per_gpu": PAIRS, "batch": BATCH, "length": LENGTH,
+                       "edit_prob": EDIT_P, "seed": SEED, "cigar_stride": CIGAR_STRIDE,
+                       "l2": "inputs larger than L2: steps cycle over 10 batches (300 MB ASCII, 152 MB CIGAR slots)",
+                       "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": f"tier_kernel tier {top}", "alg_bytes_per_launch": alg_bytes,
+                         "launch_ms": launch_ms},
+            "cpu_baseline": base,
+            "e2e": e2e,
+            "gpu_launches": gpu_launches,
+            "clocks": clocks.summary(),
+            "tiers": {"launches": st["tier_launches"][:5], "ms": [round(x, 4) for x in tier_ms[:5]],
+                      "passed_on": st["tier_passed"][:5]},
+        }
+        print(json.dumps(line))
+    ctx.close()
+    ctx2.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

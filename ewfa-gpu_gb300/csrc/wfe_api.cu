@@ -1,0 +1,510 @@
+/*
+ * wfe_api.cu -- the C ABI of libwfe (include/wfe.h): contexts, the batch
+ * pipeline of the host-buffer calls, and the device-buffer calls.
+ *
+ * The reference's batch loop (src/wavefront.cu:127-330) runs, per host
+ * thread, one batch at a time: H2D of the next batch on a second stream
+ * overlaps the current kernels, then a synchronous D2H of the CIGARs.  Here
+ * a context keeps two pipeline stages, each with its own stream and device
+ * buffers, so the copies in and out of one batch overlap the kernels of the
+ * other; the tier chain of each batch runs on its stage's stream with no host
+ * synchronisation between kernels.
+ */
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "wfe.h"
+#include "wfe_kernels.cuh"
+
+using namespace wfe;
+
+namespace {
+
+constexpr int kStages = 2;
+
+struct Stage {
+    cudaStream_t stream = nullptr;
+    char* d_ascii = nullptr;
+    size_t ascii_cap = 0;
+    wfe_pair* d_pairs = nullptr;
+    uint32_t* d_plen = nullptr;
+    uint32_t* d_tlen = nullptr;
+    int32_t* d_dist = nullptr;
+    int8_t* d_cigar = nullptr;
+    uint8_t* d_status = nullptr;
+    uint32_t* d_lists = nullptr;  /* two retry lists of batch_size entries */
+    uint32_t* d_counts = nullptr; /* one retry counter per tier */
+    char* h_stage = nullptr;      /* pinned gather buffer for scattered inputs */
+    wfe_pair* h_pairs = nullptr;  /* pinned descriptors of a gathered batch */
+};
+
+thread_local int g_last_create_error = 0;
+
+}  // namespace
+
+struct TimedLaunch {
+    int tier;
+    cudaEvent_t start, stop;
+};
+
+struct wfe_ctx {
+    wfe_config cfg{};
+    int sm_count = 0;
+    int first_tier = 0;
+    int grid[kNumTiers] = {};
+    unsigned char* d_ops_scratch = nullptr;
+    size_t ops_scratch_bytes = 0;
+    unsigned long long* d_passed = nullptr; /* pairs each tier handed on, running total */
+    Stage st[kStages];
+    int last_cuda_error = 0;
+    wfe_stats stats{};
+    std::vector<TimedLaunch> timed;      /* launches whose events are not read yet */
+    std::vector<cudaEvent_t> event_pool;
+};
+
+namespace {
+
+int fail_cuda(wfe_ctx* ctx, cudaError_t e)
+{
+    if (ctx) ctx->last_cuda_error = (int)e;
+    return e == cudaErrorMemoryAllocation ? WFE_ERR_OUT_OF_MEMORY : WFE_ERR_CUDA;
+}
+
+#define WFE_CUDA(ctx, call)                                        \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) return fail_cuda((ctx), e_);        \
+    } while (0)
+
+uint32_t default_cigar_stride(uint32_t max_seq_len)
+{
+    /* src/wavefront.cuh:48-50: seq_len + (4 - seq_len % 4) */
+    return max_seq_len + (4u - max_seq_len % 4u);
+}
+
+/* First tier by sequence length: short reads almost always finish in the
+ * 8-lane tier; long reads start where their distances usually are. */
+int default_first_tier(uint32_t max_len)
+{
+    if (max_len <= 400) return 0;
+    if (max_len <= 2000) return 2;
+    return 3;
+}
+
+void free_stage(Stage& s)
+{
+    cudaFree(s.d_ascii);
+    cudaFree(s.d_pairs);
+    cudaFree(s.d_plen);
+    cudaFree(s.d_tlen);
+    cudaFree(s.d_dist);
+    cudaFree(s.d_cigar);
+    cudaFree(s.d_status);
+    cudaFree(s.d_lists);
+    cudaFree(s.d_counts);
+    cudaFreeHost(s.h_stage);
+    cudaFreeHost(s.h_pairs);
+    if (s.stream) cudaStreamDestroy(s.stream);
+    s = Stage();
+}
+
+/* Enqueue the tier chain for work items 0..n-1 of one batch on stream s. */
+int run_chain(wfe_ctx* ctx, Stage& st, const Layout& L, uint32_t n, int32_t* dist, int8_t* cigar,
+              uint8_t* status, cudaStream_t s)
+{
+    if (n == 0) return WFE_OK;
+    const wfe_config& c = ctx->cfg;
+    WFE_CUDA(ctx, cudaMemsetAsync(st.d_counts, 0, sizeof(uint32_t) * kNumTiers, s));
+    const uint32_t B = c.batch_size;
+    for (int t = ctx->first_tier; t < kNumTiers; ++t) {
+        AlignLaunch a{};
+        a.L = L;
+        const int k = t - ctx->first_tier;
+        if (k == 0) {
+            a.work = nullptr;
+            a.work_count = nullptr;
+            a.n_work = n;
+        } else {
+            a.work = st.d_lists + (size_t)((k - 1) & 1) * B;
+            a.work_count = st.d_counts + (t - 1);
+            a.n_work = n;
+        }
+        a.dist = dist;
+        a.cigar = cigar;
+        a.cigar_stride = c.cigar_stride;
+        a.status = status;
+        a.max_distance = c.max_distance;
+        a.max_len = c.max_seq_len;
+        a.retry = (t + 1 < kNumTiers) ? st.d_lists + (size_t)(k & 1) * B : nullptr;
+        a.retry_count = st.d_counts + t;
+        a.ops_scratch = ctx->d_ops_scratch;
+        a.ops_scratch_bytes = ctx->ops_scratch_bytes;
+        /* the first tier is sized to the batch; later tiers run persistent
+         * grids that read their work count on the device */
+        int grid = ctx->grid[t];
+        if (k == 0) {
+            const TierInfo& ti = tier_info(t);
+            const uint32_t per_cta = 4u * (32u / (uint32_t)ti.G);
+            grid = (int)std::min<uint64_t>((uint64_t)grid, ((uint64_t)n + per_cta - 1) / per_cta);
+            grid = std::max(grid, 1);
+        }
+        a.passed_total = ctx->d_passed + t;
+        TimedLaunch tl{t, nullptr, nullptr};
+        const bool timing = (c.flags & WFE_FLAG_KERNEL_TIMING) != 0;
+        if (timing) {
+            for (cudaEvent_t* ev : {&tl.start, &tl.stop}) {
+                if (!ctx->event_pool.empty()) {
+                    *ev = ctx->event_pool.back();
+                    ctx->event_pool.pop_back();
+                } else {
+                    WFE_CUDA(ctx, cudaEventCreate(ev));
+                }
+            }
+            WFE_CUDA(ctx, cudaEventRecord(tl.start, s));
+        }
+        WFE_CUDA(ctx, launch_tier(t, a, grid, s));
+        if (timing) {
+            WFE_CUDA(ctx, cudaEventRecord(tl.stop, s));
+            ctx->timed.push_back(tl);
+        }
+        ctx->stats.kernel_launches++;
+        ctx->stats.tier_launches[t]++;
+        if (k == 0) ctx->stats.tier_entered[t] += n;
+        /* a distance cap below the tier's capacity ends the chain */
+        if (c.max_distance > 0 && c.max_distance <= tier_info(t).dcap) break;
+    }
+    return WFE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* wfe_strerror(int status)
+{
+    switch (status) {
+    case WFE_OK: return "success";
+    case WFE_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case WFE_ERR_OUT_OF_MEMORY: return "out of memory";
+    case WFE_ERR_SEQ_TOO_LONG: return "sequence longer than the context's max_seq_len";
+    case WFE_ERR_CUDA: return "CUDA runtime error";
+    case WFE_ERR_NO_DEVICE: return "no CUDA device";
+    case WFE_ERR_TIMEOUT: return "timed out";
+    case WFE_ERR_BUSY: return "not enough free device memory";
+    case WFE_ERR_INTERNAL: return "internal consistency check failed";
+    case WFE_ERR_NOT_FOUND: return "unknown ticket";
+    default: return "unknown status";
+    }
+}
+
+int wfe_last_cuda_error(const wfe_ctx* ctx) { return ctx ? ctx->last_cuda_error : g_last_create_error; }
+
+int wfe_create(const wfe_config* cfg, wfe_ctx** out)
+{
+    if (!cfg || !out) return WFE_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (cfg->max_seq_len == 0 || cfg->max_distance < 0) return WFE_ERR_INVALID_ARGUMENT;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        g_last_create_error = (int)e;
+        return WFE_ERR_NO_DEVICE;
+    }
+    if (cfg->device < 0 || cfg->device >= ndev) return WFE_ERR_INVALID_ARGUMENT;
+    e = cudaSetDevice(cfg->device);
+    if (e != cudaSuccess) { g_last_create_error = (int)e; return WFE_ERR_CUDA; }
+
+    wfe_ctx* ctx = new (std::nothrow) wfe_ctx();
+    if (!ctx) return WFE_ERR_OUT_OF_MEMORY;
+    ctx->cfg = *cfg;
+    wfe_config& c = ctx->cfg;
+    if (c.batch_size == 0) c.batch_size = 100000;
+    if (c.cigar_stride == 0) c.cigar_stride = default_cigar_stride(c.max_seq_len);
+    ctx->first_tier = default_first_tier(c.max_seq_len);
+
+    auto bail = [&](cudaError_t err) {
+        g_last_create_error = (int)err;
+        for (auto& s : ctx->st) free_stage(s);
+        cudaFree(ctx->d_ops_scratch);
+        cudaFree(ctx->d_passed);
+        delete ctx;
+        return err == cudaErrorMemoryAllocation ? WFE_ERR_OUT_OF_MEMORY : WFE_ERR_CUDA;
+    };
+
+    e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, c.device);
+    if (e != cudaSuccess) return bail(e);
+    size_t scratch = 0;
+    for (int t = 0; t < kNumTiers; ++t) {
+        ctx->grid[t] = tier_grid(t, c.max_seq_len, c.cigar_stride, ctx->sm_count);
+        if (ctx->grid[t] <= 0) { /* sequences too long for this tier's shared memory */
+            if (t >= ctx->first_tier) return bail(cudaErrorInvalidValue);
+            continue;
+        }
+        scratch = std::max(scratch, tier_scratch_bytes(t, ctx->grid[t]));
+    }
+    if (scratch) {
+        e = cudaMalloc(&ctx->d_ops_scratch, scratch);
+        if (e != cudaSuccess) return bail(e);
+        ctx->ops_scratch_bytes = scratch;
+    }
+    if ((e = cudaMalloc(&ctx->d_passed, sizeof(unsigned long long) * kNumTiers)) != cudaSuccess) return bail(e);
+    if ((e = cudaMemset(ctx->d_passed, 0, sizeof(unsigned long long) * kNumTiers)) != cudaSuccess) return bail(e);
+    const size_t B = c.batch_size;
+    for (auto& s : ctx->st) {
+        s.ascii_cap = B * 2u * (size_t)c.max_seq_len + 64u;
+        if ((e = cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e);
+        if ((e = cudaMalloc(&s.d_ascii, s.ascii_cap)) != cudaSuccess) return bail(e);
+        if ((e = cudaMalloc(&s.d_pairs, B * sizeof(wfe_pair))) != cudaSuccess) return bail(e);
+        if ((e = cudaMalloc(&s.d_plen, B * sizeof(uint32_t))) != cudaSuccess) return bail(e);
+        if ((e = cudaMalloc(&s.d_tlen, B * sizeof(uint32_t))) != cudaSuccess) return bail(e);
+        if ((e = cudaMalloc(&s.d_dist, B * sizeof(int32_t))) != cudaSuccess) return bail(e);
+        if ((e = cudaMalloc(&s.d_cigar, B * (size_t)c.cigar_stride + 16u)) != cudaSuccess) return bail(e);
+        if ((e = cudaMalloc(&s.d_status, B)) != cudaSuccess) return bail(e);
+        if ((e = cudaMalloc(&s.d_lists, 2u * B * sizeof(uint32_t))) != cudaSuccess) return bail(e);
+        if ((e = cudaMalloc(&s.d_counts, sizeof(uint32_t) * kNumTiers)) != cudaSuccess) return bail(e);
+    }
+    *out = ctx;
+    return WFE_OK;
+}
+
+void wfe_destroy(wfe_ctx* ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->cfg.device);
+    for (auto& s : ctx->st) {
+        if (s.stream) cudaStreamSynchronize(s.stream);
+        free_stage(s);
+    }
+    cudaFree(ctx->d_ops_scratch);
+    cudaFree(ctx->d_passed);
+    for (auto& t : ctx->timed) {
+        cudaEventDestroy(t.start);
+        cudaEventDestroy(t.stop);
+    }
+    for (auto ev : ctx->event_pool) cudaEventDestroy(ev);
+    delete ctx;
+}
+
+int wfe_get_stats(wfe_ctx* ctx, wfe_stats* out)
+{
+    if (!ctx || !out) return WFE_ERR_INVALID_ARGUMENT;
+    WFE_CUDA(ctx, cudaSetDevice(ctx->cfg.device));
+    for (auto& s : ctx->st) WFE_CUDA(ctx, cudaStreamSynchronize(s.stream));
+    for (auto& t : ctx->timed) {
+        WFE_CUDA(ctx, cudaEventSynchronize(t.stop));
+        float ms = 0.f;
+        WFE_CUDA(ctx, cudaEventElapsedTime(&ms, t.start, t.stop));
+        ctx->stats.tier_ms[t.tier] += ms;
+        ctx->event_pool.push_back(t.start);
+        ctx->event_pool.push_back(t.stop);
+    }
+    ctx->timed.clear();
+    unsigned long long passed[kNumTiers] = {};
+    WFE_CUDA(ctx, cudaMemcpy(passed, ctx->d_passed, sizeof(passed), cudaMemcpyDeviceToHost));
+    *out = ctx->stats;
+    for (int t = 0; t < kNumTiers; ++t) {
+        out->tier_passed[t] = passed[t];
+        if (t > ctx->first_tier) out->tier_entered[t] = passed[t - 1];
+    }
+    return WFE_OK;
+}
+
+int wfe_reset_stats(wfe_ctx* ctx)
+{
+    if (!ctx) return WFE_ERR_INVALID_ARGUMENT;
+    wfe_stats tmp;
+    const int r = wfe_get_stats(ctx, &tmp); /* drains pending timings */
+    if (r != WFE_OK) return r;
+    ctx->stats = wfe_stats{};
+    WFE_CUDA(ctx, cudaMemset(ctx->d_passed, 0, sizeof(unsigned long long) * kNumTiers));
+    return WFE_OK;
+}
+
+int wfe_align_device(wfe_ctx* ctx, const char* d_ascii, const wfe_pair* d_pairs, size_t n,
+                     uint32_t max_len, int32_t* d_dist, int8_t* d_cigar, uint8_t* d_status,
+                     void* stream)
+{
+    if (!ctx || (n && (!d_ascii || !d_pairs || !d_dist || (!d_cigar && ctx->cfg.cigar_stride))))
+        return WFE_ERR_INVALID_ARGUMENT;
+    if (max_len > ctx->cfg.max_seq_len) return WFE_ERR_SEQ_TOO_LONG;
+    WFE_CUDA(ctx, cudaSetDevice(ctx->cfg.device));
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->st[0].stream;
+    const size_t B = ctx->cfg.batch_size;
+    for (size_t b0 = 0; b0 < n; b0 += B) {
+        const uint32_t nb = (uint32_t)std::min(B, n - b0);
+        Layout L{};
+        L.ascii = d_ascii;
+        L.pairs = d_pairs + b0;
+        L.base_off = 0;
+        const int r = run_chain(ctx, ctx->st[0], L, nb, d_dist + b0,
+                                d_cigar ? d_cigar + b0 * ctx->cfg.cigar_stride : nullptr,
+                                d_status ? d_status + b0 : nullptr, s);
+        if (r != WFE_OK) return r;
+        ctx->stats.batches++;
+        ctx->stats.pairs += nb;
+    }
+    return WFE_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+/* Host-buffer pipeline shared by wfe_align and wfe_align_strided. */
+struct HostJob {
+    const char* ascii;
+    size_t ascii_bytes;
+    const wfe_pair* pairs;   /* descriptor layout */
+    size_t stride;           /* strided layout when pairs == NULL */
+    const uint32_t* p_len;
+    const uint32_t* t_len;
+};
+
+int align_host(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, int8_t* cigar_out,
+               uint8_t* status_out)
+{
+    const wfe_config& c = ctx->cfg;
+    WFE_CUDA(ctx, cudaSetDevice(c.device));
+    const size_t B = c.batch_size;
+    const int nstages = (c.flags & WFE_FLAG_NO_PIPELINE) ? 1 : kStages;
+    size_t bi = 0;
+    for (size_t b0 = 0; b0 < n; b0 += B, ++bi) {
+        Stage& st = ctx->st[bi % nstages];
+        cudaStream_t s = st.stream;
+        const size_t nb = std::min(B, n - b0);
+        Layout L{};
+        if (job.pairs) {
+            const wfe_pair* P = job.pairs + b0;
+            uint64_t lo = UINT64_MAX, hi = 0, bases = 0;
+            for (size_t i = 0; i < nb; ++i) {
+                if (P[i].p_len > c.max_seq_len || P[i].t_len > c.max_seq_len) return WFE_ERR_SEQ_TOO_LONG;
+                const uint64_t pe = P[i].p_off + P[i].p_len, te = P[i].t_off + P[i].t_len;
+                if (pe > job.ascii_bytes || te > job.ascii_bytes) return WFE_ERR_INVALID_ARGUMENT;
+                lo = std::min(lo, std::min(P[i].p_off, P[i].t_off));
+                hi = std::max(hi, std::max(pe, te));
+                bases += (uint64_t)P[i].p_len + P[i].t_len;
+            }
+            if (nb == 0 || hi <= lo) lo = hi = 0;
+            if (hi - lo + 32u <= st.ascii_cap) {
+                /* one contiguous copy of the batch's span */
+                WFE_CUDA(ctx, cudaMemcpyAsync(st.d_ascii, job.ascii + lo, hi - lo, cudaMemcpyHostToDevice, s));
+                WFE_CUDA(ctx, cudaMemcpyAsync(st.d_pairs, P, nb * sizeof(wfe_pair), cudaMemcpyHostToDevice, s));
+                ctx->stats.h2d_bytes += (hi - lo) + nb * sizeof(wfe_pair);
+                L.base_off = lo;
+            } else {
+                /* scattered inputs: gather this batch through pinned memory */
+                WFE_CUDA(ctx, cudaStreamSynchronize(s));
+                if (!st.h_stage) {
+                    WFE_CUDA(ctx, cudaMallocHost(&st.h_stage, st.ascii_cap));
+                    WFE_CUDA(ctx, cudaMallocHost(&st.h_pairs, B * sizeof(wfe_pair)));
+                }
+                uint64_t pos = 0;
+                for (size_t i = 0; i < nb; ++i) {
+                    wfe_pair q = P[i];
+                    std::memcpy(st.h_stage + pos, job.ascii + q.p_off, q.p_len);
+                    q.p_off = pos;
+                    pos += q.p_len;
+                    std::memcpy(st.h_stage + pos, job.ascii + q.t_off, q.t_len);
+                    q.t_off = pos;
+                    pos += q.t_len;
+                    st.h_pairs[i] = q;
+                }
+                WFE_CUDA(ctx, cudaMemcpyAsync(st.d_ascii, st.h_stage, pos, cudaMemcpyHostToDevice, s));
+                WFE_CUDA(ctx, cudaMemcpyAsync(st.d_pairs, st.h_pairs, nb * sizeof(wfe_pair), cudaMemcpyHostToDevice, s));
+                ctx->stats.h2d_bytes += pos + nb * sizeof(wfe_pair);
+                L.base_off = 0;
+                (void)bases;
+            }
+            L.ascii = st.d_ascii;
+            L.pairs = st.d_pairs;
+        } else {
+            for (size_t i = 0; i < nb; ++i)
+                if (job.p_len[b0 + i] > job.stride || job.t_len[b0 + i] > job.stride ||
+                    job.p_len[b0 + i] > c.max_seq_len || job.t_len[b0 + i] > c.max_seq_len)
+                    return WFE_ERR_SEQ_TOO_LONG;
+            const size_t bytes = 2u * nb * job.stride;
+            if (bytes + 32u > st.ascii_cap) return WFE_ERR_INVALID_ARGUMENT;
+            WFE_CUDA(ctx, cudaMemcpyAsync(st.d_ascii, job.ascii + 2u * b0 * job.stride, bytes,
+                                          cudaMemcpyHostToDevice, s));
+            WFE_CUDA(ctx, cudaMemcpyAsync(st.d_plen, job.p_len + b0, nb * 4u, cudaMemcpyHostToDevice, s));
+            WFE_CUDA(ctx, cudaMemcpyAsync(st.d_tlen, job.t_len + b0, nb * 4u, cudaMemcpyHostToDevice, s));
+            ctx->stats.h2d_bytes += bytes + nb * 8u;
+            L.ascii = st.d_ascii;
+            L.pairs = nullptr;
+            L.plen = st.d_plen;
+            L.tlen = st.d_tlen;
+            L.stride = job.stride;
+        }
+        const int r = run_chain(ctx, st, L, (uint32_t)nb, st.d_dist, st.d_cigar, st.d_status, s);
+        if (r != WFE_OK) return r;
+        WFE_CUDA(ctx, cudaMemcpyAsync(dist_out + b0, st.d_dist, nb * 4u, cudaMemcpyDeviceToHost, s));
+        ctx->stats.d2h_bytes += nb * 4u;
+        if (status_out) {
+            WFE_CUDA(ctx, cudaMemcpyAsync(status_out + b0, st.d_status, nb, cudaMemcpyDeviceToHost, s));
+            ctx->stats.d2h_bytes += nb;
+        }
+        if (cigar_out && c.cigar_stride) {
+            WFE_CUDA(ctx, cudaMemcpyAsync(cigar_out + b0 * c.cigar_stride, st.d_cigar, nb * c.cigar_stride,
+                                          cudaMemcpyDeviceToHost, s));
+            ctx->stats.d2h_bytes += nb * c.cigar_stride;
+        }
+        ctx->stats.batches++;
+        ctx->stats.pairs += nb;
+    }
+    for (int i = 0; i < nstages; ++i) WFE_CUDA(ctx, cudaStreamSynchronize(ctx->st[i].stream));
+    return WFE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int wfe_align(wfe_ctx* ctx, const char* ascii, size_t ascii_bytes, const wfe_pair* pairs, size_t n,
+              int32_t* dist_out, int8_t* cigar_out, uint8_t* status_out)
+{
+    if (!ctx || (n && (!ascii || !pairs || !dist_out))) return WFE_ERR_INVALID_ARGUMENT;
+    HostJob j{ascii, ascii_bytes, pairs, 0, nullptr, nullptr};
+    return align_host(ctx, j, n, dist_out, cigar_out, status_out);
+}
+
+int wfe_align_strided(wfe_ctx* ctx, const char* ascii, size_t stride, const uint32_t* p_len,
+                      const uint32_t* t_len, size_t n, int32_t* dist_out, int8_t* cigar_out,
+                      uint8_t* status_out)
+{
+    if (!ctx || (n && (!ascii || !p_len || !t_len || !dist_out || stride == 0)))
+        return WFE_ERR_INVALID_ARGUMENT;
+    HostJob j{ascii, 2u * n * stride, nullptr, stride, p_len, t_len};
+    return align_host(ctx, j, n, dist_out, cigar_out, status_out);
+}
+
+int wfe_pack_device(const char* d_ascii, const wfe_pair* d_pairs, size_t n, uint32_t* d_words,
+                    uint32_t words_per_seq, void* stream)
+{
+    if (n && (!d_ascii || !d_pairs || !d_words || words_per_seq == 0)) return WFE_ERR_INVALID_ARGUMENT;
+    Layout L{};
+    L.ascii = d_ascii;
+    L.pairs = d_pairs;
+    const cudaError_t e = launch_pack(L, (uint32_t)n, d_words, words_per_seq, (cudaStream_t)stream);
+    return e == cudaSuccess ? WFE_OK : WFE_ERR_CUDA;
+}
+
+int wfe_cigar_from_history_device(const char* d_ascii, const wfe_pair* d_pairs, size_t n,
+                                  uint32_t max_len, const int32_t* d_dist, const uint64_t* d_history,
+                                  int8_t* d_cigar, uint32_t cigar_stride, uint8_t* d_status,
+                                  void* stream)
+{
+    if (n && (!d_ascii || !d_pairs || !d_dist || !d_history || (!d_cigar && cigar_stride)))
+        return WFE_ERR_INVALID_ARGUMENT;
+    Layout L{};
+    L.ascii = d_ascii;
+    L.pairs = d_pairs;
+    const cudaError_t e = launch_cigar_from_history(L, (uint32_t)n, max_len, d_dist, d_history, d_cigar,
+                                                    cigar_stride, d_status, (cudaStream_t)stream);
+    return e == cudaSuccess ? WFE_OK : WFE_ERR_CUDA;
+}
+
+}  // extern "C"

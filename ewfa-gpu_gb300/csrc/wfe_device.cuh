@@ -1,0 +1,268 @@
+/*
+ * wfe_device.cuh -- device building blocks shared by the libwfe kernels.
+ *
+ * Packed sequence layout (the reference's, src/kernels.cu:313-394): 16 bases
+ * per 32-bit word, base i at bits 31-2(i%16)..30-2(i%16) of word i/16, 2-bit
+ * code (c & 6) >> 1 (src/wavefront_structures.h:73-83).
+ *
+ * In shared memory a sequence is kept as "overlapped pairs": Q[w] = {x:
+ * W[w+1], y: W[w]}, so the 16-base window starting at any base v is one
+ * 64-bit load and one funnel shift: window(v) = funnelshift_l(Q[v/16].x,
+ * Q[v/16].y, 2*(v%16)).
+ */
+#ifndef WFE_DEVICE_CUH
+#define WFE_DEVICE_CUH
+
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+#include "wfe.h"
+
+namespace wfe {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+/* Operation codes (src/wavefront_structures.h:66-71). */
+constexpr int kOpIns = 1, kOpSub = 2, kOpDel = 3;
+
+/* Four ASCII bytes (first base in the low byte) -> one byte c0c1c2c3 with
+ * c0 in bits 7:6.  The multiply gathers the four 2-bit codes, which sit at
+ * bits 0, 8, 16, 24, into bits 30, 28, 26, 24 without carries. */
+__device__ __forceinline__ uint32_t pack4(uint32_t w)
+{
+    const uint32_t x = (w & 0x06060606u) >> 1;
+    return (x * 0x40100401u) >> 24;
+}
+
+/* Sixteen ASCII bytes -> one packed word. */
+__device__ __forceinline__ uint32_t pack16(uint4 b)
+{
+    return (pack4(b.x) << 24) | (pack4(b.y) << 16) | (pack4(b.z) << 8) | pack4(b.w);
+}
+
+/* Where the bases of pair i live. */
+struct Layout {
+    const char* ascii;      /* device ASCII buffer */
+    const wfe_pair* pairs;  /* descriptor layout; NULL = strided layout */
+    const uint32_t* plen;   /* strided layout lengths */
+    const uint32_t* tlen;
+    uint64_t stride;        /* strided layout: pattern i at 2*i*stride, text at (2i+1)*stride */
+    uint64_t base_off;      /* descriptor offsets are relative to ascii - base_off */
+};
+
+struct PairRef {
+    const char* p;
+    const char* t;
+    uint32_t plen, tlen;
+};
+
+__device__ __forceinline__ PairRef get_pair(const Layout& L, uint32_t i)
+{
+    PairRef r;
+    if (L.pairs) {
+        const wfe_pair d = L.pairs[i];
+        r.p = L.ascii + (d.p_off - L.base_off);
+        r.t = L.ascii + (d.t_off - L.base_off);
+        r.plen = d.p_len;
+        r.tlen = d.t_len;
+    } else {
+        r.p = L.ascii + 2ull * i * L.stride;
+        r.t = r.p + L.stride;
+        r.plen = L.plen[i];
+        r.tlen = L.tlen[i];
+    }
+    return r;
+}
+
+/* Packed word w of a sequence of len bytes at s, produced by a group of G
+ * lanes, words w0+g for g in [0, G).  The sequence is read in aligned 16-byte
+ * blocks (every block holds at least one base of the sequence); the bytes
+ * before s are shifted out and the bases at or past len are cleared.
+ * Returns the word for lane g (0 if w0+g >= nw).  All lanes of `mask` call. */
+template <int G>
+__device__ __forceinline__ uint32_t packed_word(const char* s, uint32_t len,
+                                                uint32_t w0, int g, unsigned mask)
+{
+    const uint32_t nw = (len + 15u) >> 4;
+    const uintptr_t a = reinterpret_cast<uintptr_t>(s);
+    const uint32_t sh = (uint32_t)(a & 15u);
+    const uint4* base = reinterpret_cast<const uint4*>(a - sh);
+    const uint32_t nblk = (sh + len + 15u) >> 4;
+    const uint32_t w = w0 + (uint32_t)g;
+    uint32_t x0 = 0;
+    if (w < nw) x0 = pack16(__ldg(base + w));
+    const uint32_t nb = __shfl_down_sync(mask, x0, 1, G);
+    uint32_t W = x0;
+    if (sh != 0) {
+        uint32_t x1 = nb;
+        if (g == G - 1 || w + 1 >= nw) x1 = (w + 1 < nblk) ? pack16(__ldg(base + w + 1)) : 0u;
+        W = __funnelshift_l(x1, x0, 2u * sh);
+    }
+    if (w < nw) {
+        const uint32_t r = len - 16u * w;
+        if (r < 16u) W &= ~0u << (2u * (16u - r));
+    } else {
+        W = 0;
+    }
+    return W;
+}
+
+/* Pack a sequence into overlapped pairs Q[0..nw) (see top of file) by a
+ * group of G lanes; Q[nw-1].x = 0.  The caller syncs the group afterwards. */
+template <int G>
+__device__ __forceinline__ void load_packed(const char* s, uint32_t len, uint2* Q,
+                                            int g, unsigned mask)
+{
+    const uint32_t nw = (len + 15u) >> 4;
+    for (uint32_t w0 = 0; w0 < nw; w0 += G) {
+        const uint32_t W = packed_word<G>(s, len, w0, g, mask);
+        const uint32_t w = w0 + (uint32_t)g;
+        if (w < nw) {
+            Q[w].y = W;
+            if (w > 0) Q[w - 1].x = W;
+        }
+    }
+    if (g == 0 && nw > 0) Q[nw - 1].x = 0u;
+}
+
+/* 16-base window of a packed sequence starting at base v. */
+__device__ __forceinline__ uint32_t window(const uint2* Q, int v)
+{
+    const uint2 q = Q[v >> 4];
+    return __funnelshift_l(q.x, q.y, (uint32_t)(v & 15) << 1);
+}
+
+/* Extend along diagonal k from offset off (src/kernels.cu:27-109): the
+ * longest common prefix of pattern[v..] and text[h..], v = off - k, h = off,
+ * bounded by both lengths, 16 bases per trip.  Returns the new offset. */
+__device__ __forceinline__ int extend_lane(const uint2* QP, const uint2* QT,
+                                           int plen, int tlen, int k, int off)
+{
+    int v = off - k, h = off;
+    /* unsigned compares: a negative position (impossible for cells inside
+     * the wavefront) can never index the shared-memory sequences */
+    while ((unsigned)v < (unsigned)plen && (unsigned)h < (unsigned)tlen) {
+        const uint32_t x = window(QP, v) ^ window(QT, h);
+        int n = __clz(x) >> 1;
+        n = min(n, min(plen - v, tlen - h));
+        v += n;
+        h += n;
+        if (n < 16) break;
+    }
+    return h;
+}
+
+/* The same longest common prefix computed by a group of G lanes at once:
+ * lane g compares the window 16*g bases further on, a ballot finds the first
+ * window that is not a full match.  Returns the run length.  All lanes of
+ * the group call with the same arguments. */
+template <int G>
+__device__ __forceinline__ int group_extend(const uint2* QP, const uint2* QT, int plen,
+                                            int tlen, int k, int off, int g, int grp,
+                                            unsigned gmask)
+{
+    const int v0 = off - k, h0 = off;
+    int total = 0;
+    for (;;) {
+        const int v = v0 + total + 16 * g, h = h0 + total + 16 * g;
+        int n = 0;
+        if ((unsigned)v < (unsigned)plen && (unsigned)h < (unsigned)tlen) {
+            const uint32_t x = window(QP, v) ^ window(QT, h);
+            n = min(__clz(x) >> 1, min(plen - v, tlen - h));
+        }
+        const unsigned sb = __ballot_sync(gmask, n < 16);
+        const unsigned rel = (G == 32) ? sb : ((sb >> (grp * G)) & ((1u << (G & 31)) - 1u));
+        if (rel) {
+            const int first = __ffs((int)rel) - 1;
+            const int nf = __shfl_sync(gmask, n, first, G);
+            return total + 16 * first + nf;
+        }
+        total += 16 * G;
+    }
+}
+
+/* Byte writer into a CIGAR staging buffer of `cap` bytes (src/kernels.cu:
+ * 437-446 run chunks, 456-470 operation letters). */
+struct CigarSink {
+    int8_t* buf;
+    uint32_t cap;
+    uint32_t pos;
+    __device__ __forceinline__ void put(int8_t b)
+    {
+        if (pos < cap) buf[pos] = b;
+        ++pos;
+    }
+    __device__ __forceinline__ void run(int n)
+    {
+        for (int j = 0; j < n / 127; ++j) put((int8_t)-127);
+        if (n % 127) put((int8_t)(-(n % 127)));
+    }
+};
+
+__device__ __forceinline__ int8_t op_letter(int op)
+{
+    return op == kOpDel ? (int8_t)'D' : (op == kOpSub ? (int8_t)'X' : (int8_t)'I');
+}
+
+/* Forward replay of an operation chain (src/kernels.cu:397-498) by a group:
+ * extend from (k=0, off=0), emit the run, apply op d, ..., final extend.
+ * chain[d] is the operation of score d+1.  Lane 0 writes the bytes into
+ * sink.  Returns the full CIGAR length (on every lane), or a negative value
+ * if the chain holds a code other than INS/SUB/DEL (stops there, like the
+ * reference's "Incorrect backtrace" exit, src/kernels.cu:471-478). */
+template <int G>
+__device__ __forceinline__ int replay_chain(const uint2* QP, const uint2* QT, int plen, int tlen,
+                                            const uint8_t* chain, int D, CigarSink& sink,
+                                            int g, int grp, unsigned gmask)
+{
+    int k = 0, off = 0;
+    int bad = 0;
+    for (int d = 0; d <= D; ++d) {
+        const int run = group_extend<G>(QP, QT, plen, tlen, k, off, g, grp, gmask);
+        off += run;
+        if (g == 0) sink.run(run);
+        if (d == D) break;
+        const int op = chain[d];
+        if (op == kOpDel) {
+            --k;
+        } else if (op == kOpSub) {
+            ++off;
+        } else if (op == kOpIns) {
+            ++k;
+            ++off;
+        } else {
+            bad = 1;
+            break;
+        }
+        if (g == 0) sink.put(op_letter(op));
+    }
+    const int pos = (int)__shfl_sync(gmask, sink.pos, 0, G);
+    return bad ? -1 - pos : pos;
+}
+
+/* Copy a staged CIGAR of `len` bytes (plus terminator when it fits) from
+ * shared to global memory by a group; pads to whole 32-bit words with zeros
+ * inside the slot when the slot size allows word stores. */
+template <int G>
+__device__ __forceinline__ void store_cigar(int8_t* stage, uint32_t len, uint32_t cap,
+                                            int8_t* dst, int g, unsigned gmask)
+{
+    uint32_t nbytes = len < cap ? len + 1u : cap;
+    if (g == 0 && len < cap) stage[len] = 0;
+    if ((cap & 3u) == 0u && (reinterpret_cast<uintptr_t>(dst) & 3u) == 0u) {
+        const uint32_t nwords = (nbytes + 3u) >> 2;
+        if (g == 0)
+            for (uint32_t b = nbytes; b < nwords * 4u; ++b) stage[b] = 0;
+        __syncwarp(gmask);
+        const uint32_t* s32 = reinterpret_cast<const uint32_t*>(stage);
+        uint32_t* d32 = reinterpret_cast<uint32_t*>(dst);
+        for (uint32_t i = (uint32_t)g; i < nwords; i += G) d32[i] = s32[i];
+    } else {
+        __syncwarp(gmask);
+        for (uint32_t i = (uint32_t)g; i < nbytes; i += G) dst[i] = stage[i];
+    }
+}
+
+}  // namespace wfe
+
+#endif

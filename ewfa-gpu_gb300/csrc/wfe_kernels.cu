@@ -1,0 +1,445 @@
+/*
+ * wfe_kernels.cu -- the alignment path on sm_103a.
+ *
+ *   pack_kernel          ASCII -> 2-bit words (src/kernels.cu:313-394)
+ *   tier_kernel<G,J,S>   fused load+pack, wavefront compute+extend, bit-packed
+ *                        backtrace store, backtrace and CIGAR replay for one
+ *                        pair per group of G lanes (src/kernels.cu:27-310 and
+ *                        397-625 in one kernel)
+ *   history_cigar_kernel CIGARs from the reference's 128-bit histories
+ *                        (src/kernels.cu:397-625)
+ *
+ * Wavefront layout of tier_kernel: lane g of a group holds, in register
+ * chunk c (c = 0..2J), diagonal k = G*(c-J) - G/2 + g.  Neighbours k-1 and
+ * k+1 come from one rotating shuffle each; the lanes at a chunk edge pick up
+ * the neighbouring chunk's value.  A chunk is skipped (warp-uniformly) until
+ * the wavefront [-d, d] reaches it; lanes outside [-d, d] hold -1, the
+ * reference's sentinel (src/kernels.cu:205-219).
+ *
+ * Backtrace store: per score d and chunk, two ballots give the low and high
+ * bits of the 2-bit operation of every diagonal of the chunk (2 bits per
+ * cell).  The chain is then read back from (D, kt) to (0, 0); it equals the
+ * reference's forward history, which copies the history of the source
+ * diagonal k + op - 2 and adds op at field d-1 (src/kernels.cu:154-171).
+ */
+#include "wfe_kernels.cuh"
+
+#include <algorithm>
+
+namespace wfe {
+
+namespace {
+
+constexpr int kWarps = 4;
+constexpr int kThreads = kWarps * 32;
+
+enum : int { ST_IDLE = 0, ST_RUN, ST_DONE, ST_OVERFLOW, ST_OVERMAX, ST_TOOLONG, ST_BADWALK };
+
+__host__ __device__ constexpr size_t round16(size_t x) { return (x + 15u) & ~size_t(15); }
+
+/* 2 bits per diagonal for the G diagonals of one chunk: the low bits of the
+ * operations, then the high bits. */
+template <int G> struct OpEntry;
+template <> struct OpEntry<8> {
+    using T = uint16_t;
+    static __device__ __forceinline__ void put(T* p, int i, uint32_t lo, uint32_t hi)
+    { p[i] = (T)(lo | (hi << 8)); }
+    static __device__ __forceinline__ int get(const T* p, int i, int gl)
+    { const uint32_t e = p[i]; return (int)(((e >> gl) & 1u) | (((e >> (8 + gl)) & 1u) << 1)); }
+};
+template <> struct OpEntry<16> {
+    using T = uint32_t;
+    static __device__ __forceinline__ void put(T* p, int i, uint32_t lo, uint32_t hi)
+    { p[i] = lo | (hi << 16); }
+    static __device__ __forceinline__ int get(const T* p, int i, int gl)
+    { const uint32_t e = p[i]; return (int)(((e >> gl) & 1u) | (((e >> (16 + gl)) & 1u) << 1)); }
+};
+template <> struct OpEntry<32> {
+    using T = uint2;
+    static __device__ __forceinline__ void put(T* p, int i, uint32_t lo, uint32_t hi)
+    { p[i] = make_uint2(lo, hi); }
+    static __device__ __forceinline__ int get(const T* p, int i, int gl)
+    { const uint2 e = p[i]; return (int)(((e.x >> gl) & 1u) | (((e.y >> gl) & 1u) << 1)); }
+};
+
+template <int G_, int J_, bool SMEM_OPS_>
+struct Tier {
+    static constexpr int G = G_, J = J_;
+    static constexpr bool SMEM_OPS = SMEM_OPS_;
+    static constexpr int NC = 2 * J + 1;
+    static constexpr int DCAP = G * J + G / 2 - 1;
+    static constexpr int GPW = 32 / G;
+    using OE = OpEntry<G>;
+    using E = typename OE::T;
+    static constexpr size_t ops_bytes = round16(sizeof(E) * (size_t)DCAP * NC);
+    static constexpr size_t chain_bytes = round16((size_t)DCAP + 1);
+};
+
+inline uint32_t seq_words_for(uint32_t max_len) { return std::max<uint32_t>(1u, (max_len + 15u) / 16u); }
+
+template <class T>
+size_t group_smem_bytes(uint32_t max_len, uint32_t cigar_stride)
+{
+    return 16u * (size_t)seq_words_for(max_len) + (T::SMEM_OPS ? T::ops_bytes : 0u) +
+           T::chain_bytes + round16(cigar_stride);
+}
+
+template <class T>
+size_t cta_smem_bytes(uint32_t max_len, uint32_t cigar_stride)
+{
+    return group_smem_bytes<T>(max_len, cigar_stride) * (size_t)(kWarps * T::GPW);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kThreads)
+tier_kernel(AlignLaunch A, uint32_t seq_words, uint32_t gbytes)
+{
+    constexpr int G = T::G, J = T::J, NC = T::NC, DCAP = T::DCAP, GPW = T::GPW;
+    using OE = typename T::OE;
+    using E = typename T::E;
+    extern __shared__ __align__(16) unsigned char smem[];
+
+    const int lane = (int)(threadIdx.x & 31u), warp = (int)(threadIdx.x >> 5);
+    const int g = lane & (G - 1), grp = lane / G;
+    const unsigned gmask = (G == 32) ? kFull : (((1u << (G & 31)) - 1u) << (grp * G));
+    const uint32_t gbits = (G == 32) ? kFull : ((1u << (G & 31)) - 1u);
+    const int slot = warp * GPW + grp;
+
+    unsigned char* gs = smem + (size_t)slot * gbytes;
+    uint2* QP = reinterpret_cast<uint2*>(gs);
+    uint2* QT = QP + seq_words;
+    unsigned char* cur = gs + 16u * (size_t)seq_words;
+    E* ops;
+    if constexpr (T::SMEM_OPS) {
+        ops = reinterpret_cast<E*>(cur);
+        cur += T::ops_bytes;
+    } else {
+        const size_t gslot = (size_t)blockIdx.x * (kWarps * GPW) + (size_t)slot;
+        ops = reinterpret_cast<E*>(A.ops_scratch + gslot * T::ops_bytes);
+    }
+    uint8_t* chain = cur;
+    cur += T::chain_bytes;
+    int8_t* stage = reinterpret_cast<int8_t*>(cur);
+
+    const uint32_t count = A.work_count ? min(*A.work_count, A.n_work) : A.n_work;
+    const uint32_t step = gridDim.x * (uint32_t)(kWarps * GPW);
+    for (uint32_t wb = (blockIdx.x * kWarps + (uint32_t)warp) * GPW; wb < count; wb += step) {
+        const uint32_t item = wb + (uint32_t)grp;
+        int state = ST_IDLE;
+        uint32_t pi = 0;
+        PairRef pr;
+        pr.p = nullptr; pr.t = nullptr; pr.plen = 0; pr.tlen = 0;
+        if (item < count) {
+            pi = A.work ? A.work[item] : item;
+            pr = get_pair(A.L, pi);
+            const uint32_t mx = max(pr.plen, pr.tlen);
+            state = (mx > A.max_len || mx > 16u * seq_words) ? ST_TOOLONG : ST_RUN;
+        }
+        const uint32_t lp = state == ST_RUN ? pr.plen : 0u;
+        const uint32_t lt = state == ST_RUN ? pr.tlen : 0u;
+        load_packed<G>(pr.p, lp, QP, g, gmask);
+        load_packed<G>(pr.t, lt, QT, g, gmask);
+        __syncwarp();
+
+        const int plen = (int)lp, tlen = (int)lt, kt = tlen - plen;
+        int O[NC];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) O[c] = -1;
+        int D = 0;
+        /* score 0: the lane of diagonal 0 extends from the origin
+         * (src/kernels.cu:249-258) */
+        if (state == ST_RUN && g == G / 2) O[J] = extend_lane(QP, QT, plen, tlen, 0, 0);
+        {
+            const bool hit = state == ST_RUN && g == G / 2 && kt == 0 && O[J] == tlen;
+            if (__ballot_sync(kFull, hit) & gmask) state = ST_DONE;
+        }
+        for (int d = 1;; ++d) {
+            const bool run = state == ST_RUN;
+            if (!__any_sync(kFull, run)) break;
+            if (d > DCAP || (A.max_distance > 0 && d > A.max_distance)) {
+                if (run) state = (A.max_distance > 0 && d > A.max_distance) ? ST_OVERMAX : ST_OVERFLOW;
+                break;
+            }
+            const int rowbase = (d - 1) * NC;
+            int N[NC];
+            /* compute (src/kernels.cu:129-152) */
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                const int lo_k = G * (c - J) - G / 2;
+                N[c] = -1;
+                if (lo_k <= d && lo_k + G - 1 >= -d) {
+                    const int upsrc = (c + 1 < NC) ? O[(c + 1 < NC) ? c + 1 : 0] : -1;
+                    const int dnsrc = (c > 0) ? O[(c > 0) ? c - 1 : 0] : -1;
+                    const int up = __shfl_sync(kFull, g == 0 ? upsrc : O[c], (g + 1) & (G - 1), G);
+                    const int dn = __shfl_sync(kFull, g == G - 1 ? dnsrc : O[c], (g + G - 1) & (G - 1), G);
+                    const int del_p = (int)(((unsigned)up) << 2) | kOpDel;
+                    const int sub_p = (int)(((unsigned)(O[c] + 1)) << 2) | kOpSub;
+                    const int ins_p = (int)(((unsigned)(dn + 1)) << 2) | kOpIns;
+                    const int m = max(max(del_p, sub_p), ins_p);
+                    const unsigned blo = __ballot_sync(kFull, m & 1);
+                    const unsigned bhi = __ballot_sync(kFull, m & 2);
+                    if (run && g == 0)
+                        OE::put(ops, rowbase + c, (blo >> ((grp * G) & 31)) & gbits,
+                                (bhi >> ((grp * G) & 31)) & gbits);
+                    const int k = lo_k + g;
+                    N[c] = (run && k >= -d && k <= d) ? (m >> 2) : -1;
+                }
+            }
+            /* extend and test the target (src/kernels.cu:173-176, 268) */
+            bool hit = false;
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                const int lo_k = G * (c - J) - G / 2;
+                if (lo_k <= d && lo_k + G - 1 >= -d) {
+                    const int k = lo_k + g;
+                    if (N[c] >= 0) {
+                        N[c] = extend_lane(QP, QT, plen, tlen, k, N[c]);
+                        hit |= (k == kt) && (N[c] == tlen);
+                    }
+                    O[c] = N[c];
+                }
+            }
+            if ((__ballot_sync(kFull, hit) & gmask) && run) {
+                state = ST_DONE;
+                D = d;
+            }
+        }
+
+        if (state == ST_DONE) {
+            /* backtrace: from (D, kt) back to (0, 0); a walk that leaves the
+             * wavefront (never expected) is reported, not followed */
+            int walk_ok = 1;
+            if (g == 0) {
+                int k = kt;
+                for (int s = D; s >= 1; --s) {
+                    if (k < -s || k > s) { walk_ok = 0; break; }
+                    const int idx = k + G / 2 + G * J;
+                    const int op = OE::get(ops, (s - 1) * NC + idx / G, idx & (G - 1));
+                    chain[s - 1] = (uint8_t)op;
+                    k += op - 2;
+                }
+                if (k != 0) walk_ok = 0;
+            }
+            walk_ok = __shfl_sync(gmask, walk_ok, 0, G);
+            if (!walk_ok) state = ST_BADWALK;
+        }
+        if (state == ST_DONE) {
+            __syncwarp(gmask);
+            CigarSink sink{stage, A.cigar_stride, 0u};
+            const int len = replay_chain<G>(QP, QT, plen, tlen, chain, D, sink, g, grp, gmask);
+            if (A.cigar_stride)
+                store_cigar<G>(stage, (uint32_t)len, A.cigar_stride,
+                               A.cigar + (size_t)pi * A.cigar_stride, g, gmask);
+            if (g == 0) {
+                A.dist[pi] = D;
+                if (A.status)
+                    A.status[pi] = (uint32_t)len > A.cigar_stride ? (uint8_t)WFE_PAIR_CIGAR_TRUNCATED
+                                                                  : (uint8_t)WFE_PAIR_OK;
+            }
+        } else if (state == ST_OVERFLOW && A.retry) {
+            /* hand the pair to the next tier */
+            if (g == 0) {
+                const uint32_t s = atomicAdd(A.retry_count, 1u);
+                A.retry[s] = pi;
+                if (A.passed_total) atomicAdd(A.passed_total, 1ull);
+            }
+        } else if (state == ST_OVERFLOW || state == ST_OVERMAX || state == ST_TOOLONG ||
+                   state == ST_BADWALK) {
+            if (g == 0) {
+                A.dist[pi] = state == ST_OVERMAX ? A.max_distance + 1 : -1;
+                if (A.status)
+                    A.status[pi] = state == ST_OVERMAX  ? (uint8_t)WFE_PAIR_OVER_MAX_DISTANCE
+                                   : state == ST_BADWALK ? (uint8_t)WFE_PAIR_BAD_HISTORY
+                                                         : (uint8_t)WFE_PAIR_TOO_LONG;
+                if (A.cigar_stride) A.cigar[(size_t)pi * A.cigar_stride] = 0;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+using T0 = Tier<8, 3, true>;    /* distance <= 27  */
+using T1 = Tier<32, 2, true>;   /* distance <= 79  */
+using T2 = Tier<32, 4, true>;   /* distance <= 143 */
+using T3 = Tier<32, 8, false>;  /* distance <= 271 */
+using T4 = Tier<32, 16, false>; /* distance <= 527 */
+
+const TierInfo kTiers[kNumTiers] = {
+    {T0::G, T0::J, T0::DCAP, T0::SMEM_OPS},
+    {T1::G, T1::J, T1::DCAP, T1::SMEM_OPS},
+    {T2::G, T2::J, T2::DCAP, T2::SMEM_OPS},
+    {T3::G, T3::J, T3::DCAP, T3::SMEM_OPS},
+    {T4::G, T4::J, T4::DCAP, T4::SMEM_OPS},
+};
+
+template <class T>
+int grid_of(uint32_t max_len, uint32_t cigar_stride, int sm_count)
+{
+    const size_t smem = cta_smem_bytes<T>(max_len, cigar_stride);
+    if (smem > 227u * 1024u) return 0;
+    cudaFuncSetAttribute(tier_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, tier_kernel<T>, kThreads, smem) != cudaSuccess)
+        return 0;
+    return std::max(1, nb) * sm_count;
+}
+
+template <class T>
+cudaError_t launch(const AlignLaunch& a, int grid, cudaStream_t s)
+{
+    const uint32_t sw = seq_words_for(a.max_len);
+    const size_t gb = group_smem_bytes<T>(a.max_len, a.cigar_stride);
+    const size_t smem = gb * (size_t)(kWarps * T::GPW);
+    if (smem > 227u * 1024u) return cudaErrorInvalidValue;
+    if (!T::SMEM_OPS && a.ops_scratch_bytes < T::ops_bytes * (size_t)grid * (kWarps * T::GPW))
+        return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(tier_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    tier_kernel<T><<<grid, kThreads, smem, s>>>(a, sw, (uint32_t)gb);
+    return cudaGetLastError();
+}
+
+/* ------------------------------------------------------------------------ */
+/* Standalone packer: one warp per sequence (src/kernels.cu:313-394). */
+__global__ void __launch_bounds__(256)
+pack_kernel(Layout L, uint32_t n, uint32_t* out, uint32_t wps)
+{
+    const int lane = (int)(threadIdx.x & 31u);
+    const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarp = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t sidx = wid; sidx < 2u * n; sidx += nwarp) {
+        const PairRef pr = get_pair(L, sidx >> 1);
+        const char* s = (sidx & 1u) ? pr.t : pr.p;
+        const uint32_t len = (sidx & 1u) ? pr.tlen : pr.plen;
+        uint32_t* dst = out + (size_t)sidx * wps;
+        const uint32_t nw = (len + 15u) >> 4;
+        for (uint32_t w0 = 0; w0 < wps; w0 += 32u) {
+            uint32_t W = 0;
+            if (w0 < nw) W = packed_word<32>(s, len, w0, lane, kFull);
+            if (w0 + (uint32_t)lane < wps) dst[w0 + lane] = W;
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* CIGARs from 128-bit histories (src/kernels.cu:397-625): one group of 8
+ * lanes per pair. */
+constexpr int kHG = 8;
+
+__global__ void __launch_bounds__(kThreads)
+history_cigar_kernel(Layout L, uint32_t n, uint32_t max_len, const int32_t* dist,
+                     const uint64_t* hist, int8_t* cigar, uint32_t stride, uint8_t* status,
+                     uint32_t seq_words, uint32_t gbytes)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    constexpr int G = kHG, GPW = 32 / G;
+    const int lane = (int)(threadIdx.x & 31u), warp = (int)(threadIdx.x >> 5);
+    const int g = lane & (G - 1), grp = lane / G;
+    const unsigned gmask = ((1u << G) - 1u) << (grp * G);
+    unsigned char* gs = smem + (size_t)(warp * GPW + grp) * gbytes;
+    uint2* QP = reinterpret_cast<uint2*>(gs);
+    uint2* QT = QP + seq_words;
+    uint8_t* chain = gs + 16u * (size_t)seq_words;
+    int8_t* stage = reinterpret_cast<int8_t*>(chain + 64);
+    const uint32_t step = gridDim.x * (uint32_t)(kWarps * GPW);
+    for (uint32_t wb = (blockIdx.x * kWarps + (uint32_t)warp) * GPW; wb < n; wb += step) {
+        const uint32_t pi = wb + (uint32_t)grp;
+        if (pi >= n) continue; /* whole group leaves together */
+        const PairRef pr = get_pair(L, pi);
+        const int D = dist[pi];
+        const bool toolong = max(pr.plen, pr.tlen) > max_len || max(pr.plen, pr.tlen) > 16u * seq_words;
+        if (toolong || D < 0 || D > 63) {
+            if (g == 0) {
+                if (status)
+                    status[pi] = toolong ? (uint8_t)WFE_PAIR_TOO_LONG : (uint8_t)WFE_PAIR_OVER_MAX_DISTANCE;
+                if (stride) cigar[(size_t)pi * stride] = 0;
+            }
+            continue;
+        }
+        load_packed<G>(pr.p, pr.plen, QP, g, gmask);
+        load_packed<G>(pr.t, pr.tlen, QT, g, gmask);
+        const uint64_t w0 = hist[2u * pi], w1 = hist[2u * pi + 1u];
+        for (int d = g; d < D; d += G)
+            chain[d] = (uint8_t)(((d < 32 ? w0 : w1) >> (2 * (d & 31))) & 3u);
+        __syncwarp(gmask);
+        CigarSink sink{stage, stride, 0u};
+        int len = replay_chain<G>(QP, QT, (int)pr.plen, (int)pr.tlen, chain, D, sink, g, grp, gmask);
+        const bool bad = len < 0;
+        if (bad) len = -1 - len;
+        if (stride) store_cigar<G>(stage, (uint32_t)len, stride, cigar + (size_t)pi * stride, g, gmask);
+        if (g == 0 && status)
+            status[pi] = bad ? (uint8_t)WFE_PAIR_BAD_HISTORY
+                             : ((uint32_t)len > stride ? (uint8_t)WFE_PAIR_CIGAR_TRUNCATED
+                                                       : (uint8_t)WFE_PAIR_OK);
+        __syncwarp(gmask);
+    }
+}
+
+}  // namespace
+
+const TierInfo& tier_info(int t) { return kTiers[t]; }
+
+size_t tier_scratch_bytes(int tier, int grid)
+{
+    switch (tier) {
+    case 3: return T3::ops_bytes * (size_t)grid * (kWarps * T3::GPW);
+    case 4: return T4::ops_bytes * (size_t)grid * (kWarps * T4::GPW);
+    default: return 0;
+    }
+}
+
+int tier_grid(int tier, uint32_t max_len, uint32_t cigar_stride, int sm_count)
+{
+    switch (tier) {
+    case 0: return grid_of<T0>(max_len, cigar_stride, sm_count);
+    case 1: return grid_of<T1>(max_len, cigar_stride, sm_count);
+    case 2: return grid_of<T2>(max_len, cigar_stride, sm_count);
+    case 3: return grid_of<T3>(max_len, cigar_stride, sm_count);
+    case 4: return grid_of<T4>(max_len, cigar_stride, sm_count);
+    default: return 0;
+    }
+}
+
+cudaError_t launch_tier(int tier, const AlignLaunch& a, int grid, cudaStream_t s)
+{
+    if (grid <= 0) return cudaErrorInvalidConfiguration;
+    switch (tier) {
+    case 0: return launch<T0>(a, grid, s);
+    case 1: return launch<T1>(a, grid, s);
+    case 2: return launch<T2>(a, grid, s);
+    case 3: return launch<T3>(a, grid, s);
+    case 4: return launch<T4>(a, grid, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_pack(const Layout& L, uint32_t n, uint32_t* words, uint32_t wps, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    const uint32_t warps = 2u * n;
+    const uint32_t blocks = std::min<uint32_t>((warps + 7u) / 8u, 65535u * 16u);
+    pack_kernel<<<blocks, 256, 0, s>>>(L, n, words, wps);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cigar_from_history(const Layout& L, uint32_t n, uint32_t max_len,
+                                      const int32_t* dist, const uint64_t* hist, int8_t* cigar,
+                                      uint32_t stride, uint8_t* status, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    const uint32_t sw = seq_words_for(max_len);
+    const size_t gb = 16u * (size_t)sw + 64u + round16(stride);
+    const size_t smem = gb * (size_t)(kWarps * (32 / kHG));
+    if (smem > 227u * 1024u) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(history_cigar_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    const uint32_t per_cta = kWarps * (32 / kHG);
+    const uint32_t blocks = std::min<uint32_t>((n + per_cta - 1u) / per_cta, 1u << 20);
+    history_cigar_kernel<<<blocks, kThreads, smem, s>>>(L, n, max_len, dist, hist, cigar, stride, status,
+                                                        sw, (uint32_t)gb);
+    return cudaGetLastError();
+}
+
+}  // namespace wfe

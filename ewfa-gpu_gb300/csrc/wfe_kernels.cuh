@@ -1,0 +1,61 @@
+/*
+ * wfe_kernels.cuh -- launch interface of the libwfe kernels (host side).
+ */
+#ifndef WFE_KERNELS_CUH
+#define WFE_KERNELS_CUH
+
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+#include "wfe_device.cuh"
+
+namespace wfe {
+
+/* Register tiers of the alignment kernel: G lanes per alignment, 2J+1
+ * register chunks of G diagonals per lane, largest distance G*J + G/2 - 1. */
+struct TierInfo {
+    int G, J, dcap;
+    bool ops_in_smem;
+};
+
+constexpr int kNumTiers = 5;
+const TierInfo& tier_info(int t);
+
+/* Arguments of one alignment launch over a work list. */
+struct AlignLaunch {
+    Layout L;
+    const uint32_t* work;        /* pair indices; NULL = 0..n_work-1 */
+    const uint32_t* work_count;  /* device count of `work`; NULL = n_work */
+    uint32_t n_work;             /* bound on the work list */
+    int32_t* dist;
+    int8_t* cigar;
+    uint32_t cigar_stride;
+    uint8_t* status;
+    int32_t max_distance;        /* 0 = unlimited */
+    uint32_t max_len;            /* every sequence of the launch is <= max_len */
+    uint32_t* retry;             /* pairs above the tier's distance capacity;
+                                    NULL = last tier: they get WFE_PAIR_TOO_LONG */
+    uint32_t* retry_count;
+    unsigned long long* passed_total; /* running count of pairs handed on (stats) */
+    unsigned char* ops_scratch;  /* global op store for tiers that keep it there */
+    size_t ops_scratch_bytes;
+};
+
+/* Bytes of global op-store scratch tier t needs for `grid` CTAs. */
+size_t tier_scratch_bytes(int tier, int grid);
+/* Persistent grid of tier t for sequences up to max_len, cigar slots of
+ * cigar_stride (occupancy-limited, at least 1). */
+int tier_grid(int tier, uint32_t max_len, uint32_t cigar_stride, int sm_count);
+cudaError_t launch_tier(int tier, const AlignLaunch& a, int grid, cudaStream_t s);
+
+cudaError_t launch_pack(const Layout& L, uint32_t n, uint32_t* words,
+                        uint32_t words_per_seq, cudaStream_t s);
+
+cudaError_t launch_cigar_from_history(const Layout& L, uint32_t n, uint32_t max_len,
+                                      const int32_t* dist, const uint64_t* hist,
+                                      int8_t* cigar, uint32_t cigar_stride,
+                                      uint8_t* status, cudaStream_t s);
+
+}  // namespace wfe
+
+#endif

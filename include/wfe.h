@@ -1,0 +1,212 @@
+/*
+ * wfe.h -- C ABI of libwfe, a GB300 (sm_103a) wavefront edit-distance
+ * aligner with full CIGAR output.
+ *
+ * It replaces the host/device boundary of quim0/eWFA-GPU: the class
+ * Sequences (src/wavefront.cuh:435-505, src/wavefront.cu:29-330) and the
+ * kernel ABI (src/kernels.cuh:32-54).  Results are bit-exact with the
+ * reference's algorithm: same edit distance and the same CIGAR bytes under
+ * its tie order (deletion > mismatch > insertion), encoded as the reference
+ * encodes them (src/kernels.cu:397-498): M runs as negative signed-char
+ * chunks of at most 127, then 'X', 'I', 'D' as ASCII, zero terminated when
+ * shorter than the slot (the bytes of a slot after its terminator are not
+ * specified).  'D' consumes a pattern base, 'I' a text base.
+ *
+ * Conventions: every call returns a wfe_status (never exits); the caller owns
+ * every buffer passed in, the context owns all device memory it allocates.
+ * A context is used by one host thread at a time; different contexts may be
+ * used concurrently.  No call takes torch or CUDA C++ types: streams are
+ * passed as void* (a cudaStream_t).
+ */
+#ifndef WFE_H
+#define WFE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WFE_ABI_VERSION 1
+
+/* Call status.  The reference exits the process on any CUDA error
+ * (utils/cuda_helpers.cuh:24-31) or fatal condition (utils/logger.h:66-68). */
+typedef enum wfe_status {
+    WFE_OK = 0,
+    WFE_ERR_INVALID_ARGUMENT = 1,
+    WFE_ERR_OUT_OF_MEMORY = 2,
+    WFE_ERR_SEQ_TOO_LONG = 3,    /* a sequence exceeds the context's max_seq_len */
+    WFE_ERR_CUDA = 4,            /* a CUDA runtime call failed (see wfe_last_cuda_error) */
+    WFE_ERR_NO_DEVICE = 5,
+    WFE_ERR_TIMEOUT = 6,         /* a bounded wait ran out */
+    WFE_ERR_BUSY = 7,            /* admission refused: not enough free device memory */
+    WFE_ERR_INTERNAL = 8,        /* a device-side consistency check failed */
+    WFE_ERR_NOT_FOUND = 9        /* unknown ticket */
+} wfe_status;
+
+/* Per-pair status written to status_out. */
+enum {
+    WFE_PAIR_OK = 0,
+    WFE_PAIR_OVER_MAX_DISTANCE = 1, /* distance > max_distance: distance_out =
+                                       max_distance + 1 (the reference writes 64
+                                       for its cap, src/kernels.cu:259,290), CIGAR
+                                       empty */
+    WFE_PAIR_CIGAR_TRUNCATED = 2,   /* CIGAR longer than the slot: the first
+                                       cigar_stride bytes are written, no
+                                       terminator (the reference overflows into
+                                       the next slot instead) */
+    WFE_PAIR_TOO_LONG = 3,          /* sequence longer than the launch's capacity */
+    WFE_PAIR_BAD_HISTORY = 4        /* history holds a code that is not an
+                                       operation: the CIGAR stops there (the
+                                       reference's "Incorrect backtrace" exit,
+                                       src/kernels.cu:471-478) */
+};
+
+/* One pattern/text pair inside a caller buffer of ASCII bases.  Any byte is a
+ * base: its 2-bit code is (byte & 6) >> 1, so A C T G = 0 1 2 3 and N, a, c,
+ * t, g alias to them (src/wavefront_structures.h:73-83). */
+typedef struct wfe_pair {
+    uint64_t p_off;  /* pattern: bytes [p_off, p_off + p_len) */
+    uint64_t t_off;  /* text:    bytes [t_off, t_off + t_len) */
+    uint32_t p_len;
+    uint32_t t_len;
+} wfe_pair;
+
+typedef struct wfe_config {
+    int32_t device;        /* CUDA device ordinal (the reference uses 0, src/aligner.cu:147) */
+    uint32_t max_seq_len;  /* longest pattern or text accepted, in bases */
+    uint32_t batch_size;   /* pairs per device batch (-b, src/aligner.cu:149-159);
+                              0 = 100000 */
+    int32_t max_distance;  /* largest distance searched, 0 = no limit.  63
+                              reproduces the reference's search range
+                              (src/wavefront.cuh:462-466) */
+    uint32_t cigar_stride; /* bytes per CIGAR slot; 0 = the reference's
+                              cigar_max_len for max_seq_len, l + (4 - l % 4)
+                              (src/wavefront.cuh:48-50) */
+    uint32_t flags;        /* WFE_FLAG_* */
+} wfe_config;
+
+#define WFE_FLAG_NO_PIPELINE 1u   /* host calls: one batch in flight (no copy/compute overlap) */
+#define WFE_FLAG_KERNEL_TIMING 2u /* time every kernel launch with CUDA events on its
+                                     stream; read back by wfe_get_stats */
+
+typedef struct wfe_ctx wfe_ctx;
+
+/* Counters of one context since creation (or the last reset). */
+typedef struct wfe_stats {
+    uint64_t pairs;            /* pairs aligned */
+    uint64_t batches;          /* device batches run */
+    uint64_t kernel_launches;  /* kernels launched by this context */
+    uint64_t h2d_bytes;        /* host-to-device bytes copied */
+    uint64_t d2h_bytes;        /* device-to-host bytes copied */
+    uint64_t tier_entered[8];  /* pairs that entered each distance tier */
+    uint64_t tier_passed[8];   /* pairs each tier handed on to the next (above
+                                  its distance capacity) */
+    uint64_t tier_launches[8]; /* launches of each tier's kernel */
+    double tier_ms[8];         /* GPU milliseconds of those launches (only with
+                                  WFE_FLAG_KERNEL_TIMING) */
+} wfe_stats;
+
+/* ---- lifecycle -------------------------------------------------------- */
+
+/* Create a context on cfg->device: streams, device buffers for one batch in
+ * each pipeline stage, pinned staging.  Replaces the Sequences constructor
+ * and GPU_memory_init (src/wavefront.cuh:458-485, src/wavefront.cu:29-108). */
+int wfe_create(const wfe_config* cfg, wfe_ctx** out);
+
+/* Release everything the context owns.  Replaces GPU_memory_free
+ * (src/wavefront.cu:110-125). */
+void wfe_destroy(wfe_ctx* ctx);
+
+const char* wfe_strerror(int status);
+
+/* Last CUDA runtime error code seen by ctx (0 if none); ctx may be NULL for
+ * the thread's last wfe_create failure. */
+int wfe_last_cuda_error(const wfe_ctx* ctx);
+
+/* Counters of ctx; waits for the context's outstanding device work first
+ * (the per-tier counters and timings live on the device until then). */
+int wfe_get_stats(wfe_ctx* ctx, wfe_stats* out);
+int wfe_reset_stats(wfe_ctx* ctx);
+
+/* ---- host-buffer alignment (the reference's batch loop) --------------- */
+
+/* Align n pairs held in HOST memory; results to HOST memory.  Replaces the
+ * loop GPU_launch_wavefront_distance / prepare_next_batch
+ * (src/aligner.cu:63-65, src/wavefront.cu:173-330): batches of batch_size
+ * pairs are copied in, packed, aligned, their CIGARs generated and copied
+ * back, with the copies of one batch overlapping the kernels of another.
+ * dist_out[n], cigar_out[n * cigar_stride], status_out[n] (may be NULL).
+ * Synchronous: returns when every result is in host memory. */
+int wfe_align(wfe_ctx* ctx, const char* ascii, size_t ascii_bytes,
+              const wfe_pair* pairs, size_t n, int32_t* dist_out,
+              int8_t* cigar_out, uint8_t* status_out);
+
+/* Same, with the reference reader's layout: pattern of pair i at
+ * ascii + 2*i*stride, text at ascii + (2*i+1)*stride, lengths in p_len[] and
+ * t_len[] (utils/sequence_reader.cu:148-189; WF_element,
+ * src/wavefront_structures.h:44-50). */
+int wfe_align_strided(wfe_ctx* ctx, const char* ascii, size_t stride,
+                      const uint32_t* p_len, const uint32_t* t_len, size_t n,
+                      int32_t* dist_out, int8_t* cigar_out,
+                      uint8_t* status_out);
+
+/* ---- device-buffer alignment ------------------------------------------ */
+
+/* Align n pairs whose ASCII and descriptors are already in DEVICE memory;
+ * results to DEVICE memory; enqueued on `stream` (a cudaStream_t; NULL = the
+ * context's stream), asynchronous.  max_len: an upper bound on every p_len
+ * and t_len of the call (pairs above it get WFE_PAIR_TOO_LONG).  The ASCII
+ * buffer must stay readable up to the next 16-byte boundary after every
+ * sequence (sequences are read in aligned 16-byte blocks).  Replaces the
+ * kernel chain WF_edit_distance -> generate_cigars
+ * (src/wavefront.cu:203-260). */
+int wfe_align_device(wfe_ctx* ctx, const char* d_ascii,
+                     const wfe_pair* d_pairs, size_t n, uint32_t max_len,
+                     int32_t* d_dist, int8_t* d_cigar, uint8_t* d_status,
+                     void* stream);
+
+/* Pack 2n sequences into 2-bit words on the device, the layout of the
+ * reference's compact_sequences (src/kernels.cu:313-394): 16 bases per
+ * 32-bit word, base i of a sequence at bits 31-2(i%16)..30-2(i%16) of word
+ * i/16, bases past the end 0.  Pair i: pattern words at
+ * d_words + 2*i*words_per_seq, text words at d_words + (2*i+1)*words_per_seq;
+ * words_per_seq >= ceil(max length / 16). */
+int wfe_pack_device(const char* d_ascii, const wfe_pair* d_pairs, size_t n,
+                    uint32_t* d_words, uint32_t words_per_seq, void* stream);
+
+/* Encoded CIGARs from the reference's backtrace records on the device:
+ * per pair a distance (< 64) and the 128-bit history words[2] of
+ * WF_backtrace_result_t (src/wavefront_structures.h:57-60), op d in bits
+ * 2(d%32)..2(d%32)+1 of words[d/32].  Replaces generate_cigars /
+ * generate_cigars_sh_mem (src/kernels.cu:397-625). */
+int wfe_cigar_from_history_device(const char* d_ascii, const wfe_pair* d_pairs,
+                                  size_t n, uint32_t max_len,
+                                  const int32_t* d_dist,
+                                  const uint64_t* d_history, int8_t* d_cigar,
+                                  uint32_t cigar_stride, uint8_t* d_status,
+                                  void* stream);
+
+/* ---- host CIGAR utilities ---------------------------------------------- */
+
+/* Text of one encoded CIGAR.  compat = 0: run-length form, e.g.
+ * "20M1X129M1D3M".  compat = 1: the reference's -p printer byte for byte,
+ * defects included (src/wavefront.cuh:146-184).  Returns the text length
+ * (excluding the terminator); out may be NULL to size it. */
+size_t wfe_format_cigar(const int8_t* cigar, size_t cigar_stride, char* out,
+                        size_t out_cap, int compat);
+
+/* Replay an encoded CIGAR against its pair on the host: M must match, X must
+ * mismatch, the walk must end at (p_len, t_len).  Returns 1 if valid and
+ * stores the number of X/I/D in *score.  Replaces Cigars::check_cigar
+ * (src/wavefront.cuh:297-419), the reference's DEBUG-mode validator. */
+int wfe_check_cigar(const char* pattern, uint32_t p_len, const char* text,
+                    uint32_t t_len, const int8_t* cigar, size_t cigar_stride,
+                    int32_t* score);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WFE_H */

@@ -1,0 +1,282 @@
+"""GPU parity: libwfe's CUDA path against the reference's golden vectors and
+against the CPU oracle, through the C ABI.  Integer work: every comparison is
+bit-exact (distance, status and the bytes of each CIGAR up to and including
+its terminator)."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+import wfe
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "ref_vectors.npz")
+
+
+def torch_cuda():
+    import torch
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    return torch
+
+
+@pytest.fixture(scope="module")
+def golden():
+    z = np.load(GOLDEN)
+    a = z["ascii"].tobytes()
+    seqs = [(a[o[0]:o[0] + o[1]], a[o[2]:o[2] + o[3]]) for o in z["offsets"]]
+    ascii, pairs = wfe.pairs_from_list(seqs)
+    return z, seqs, ascii, pairs
+
+
+def cigar_bytes(row):
+    """Encoded CIGAR up to and including its terminator (or the full slot)."""
+    row = np.asarray(row, dtype=np.int8)
+    nz = np.flatnonzero(row == 0)
+    return row[: nz[0] + 1].tobytes() if len(nz) else row.tobytes()
+
+
+def assert_same_cigars(got, want, idx=None):
+    idx = range(len(got)) if idx is None else idx
+    for i in idx:
+        assert cigar_bytes(got[i]) == cigar_bytes(want[i]), f"pair {i}"
+
+
+def oracle_run(ascii, pairs, stride, max_distance=0):
+    return O.align_batch(ascii, pairs["p_off"], pairs["p_len"], pairs["t_off"], pairs["t_len"], stride,
+                         max_distance=max_distance, nthreads=os.cpu_count() or 1)
+
+
+def compare_with_oracle(ascii, pairs, stride, dist, cg, st, max_distance=0):
+    od, ocg, ost, _ = oracle_run(ascii, pairs, stride, max_distance)
+    bad = np.flatnonzero((od != dist) | (ost != st))
+    assert len(bad) == 0, f"{len(bad)} pairs differ, first {bad[:5]}: gpu {dist[bad[:5]]} oracle {od[bad[:5]]}"
+    assert_same_cigars(cg, ocg)
+
+
+# ---------------------------------------------------------------------------
+# golden vectors of the reference itself
+
+def test_golden_host_api(golden):
+    """wfe_align (descriptor layout) with the reference's search range."""
+    z, seqs, ascii, pairs = golden
+    with wfe.Context(max_seq_len=300, max_distance=63, cigar_stride=152) as ctx:
+        dist, cg, st = ctx.align(ascii, pairs)
+    ok = z["dist"] < 64
+    np.testing.assert_array_equal(dist[ok], z["dist"][ok])
+    assert (st[ok] == wfe.PAIR_OK).all()
+    assert_same_cigars(cg, z["cigars"], np.flatnonzero(ok))
+    # over the reference's cap: the reference's distance 64, no CIGAR
+    assert (dist[~ok] == 64).all() and (st[~ok] == wfe.PAIR_OVER_MAX_DISTANCE).all()
+    assert (cg[~ok, 0] == 0).all()
+
+
+def test_golden_strided_reference_layout(golden):
+    """wfe_align_strided on the reference reader's buffer (304-byte slots)."""
+    z, seqs, _, _ = golden
+    unp = 150 * 2 + (4 - (150 * 2) % 4)
+    buf = np.zeros(2 * unp * len(seqs), dtype=np.uint8)
+    for i, (p, t) in enumerate(seqs):
+        buf[2 * i * unp: 2 * i * unp + len(p)] = np.frombuffer(p, np.uint8)
+        buf[(2 * i + 1) * unp: (2 * i + 1) * unp + len(t)] = np.frombuffer(t, np.uint8)
+    pl = np.array([len(p) for p, _ in seqs], np.uint32)
+    tl = np.array([len(t) for _, t in seqs], np.uint32)
+    with wfe.Context(max_seq_len=300, max_distance=63, cigar_stride=152, batch_size=128) as ctx:
+        dist, cg, st = ctx.align_strided(buf, unp, pl, tl)
+    ok = z["dist"] < 64
+    np.testing.assert_array_equal(dist[ok], z["dist"][ok])
+    assert_same_cigars(cg, z["cigars"], np.flatnonzero(ok))
+
+
+def test_golden_unlimited_distance(golden):
+    """No cap: every pair, the 18 over the reference's cap included, gets
+    the oracle's distance and CIGAR."""
+    z, seqs, ascii, pairs = golden
+    with wfe.Context(max_seq_len=300, cigar_stride=400) as ctx:
+        dist, cg, st = ctx.align(ascii, pairs)
+    compare_with_oracle(ascii, pairs, 400, dist, cg, st)
+    assert (dist[z["dist"] >= 64] >= 64).all()
+    for i, (p, t) in enumerate(seqs):
+        assert O.levenshtein(p, t) == dist[i]
+
+
+def test_golden_device_api_and_pack(golden):
+    torch = torch_cuda()
+    z, seqs, ascii, pairs = golden
+    n = len(seqs)
+    d_ascii = torch.from_numpy(ascii).cuda()
+    d_pairs = torch.from_numpy(pairs.view(np.uint8)).cuda()
+    d_dist = torch.zeros(n, dtype=torch.int32, device="cuda")
+    d_cg = torch.zeros(n * 152, dtype=torch.int8, device="cuda")
+    d_st = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    with wfe.Context(max_seq_len=300, max_distance=63, cigar_stride=152) as ctx:
+        ctx.align_device(d_ascii, d_pairs, n, 300, d_dist, d_cg, d_st, torch.cuda.current_stream())
+        torch.cuda.synchronize()
+    dist = d_dist.cpu().numpy()
+    cg = d_cg.cpu().numpy().reshape(n, 152)
+    ok = z["dist"] < 64
+    np.testing.assert_array_equal(dist[ok], z["dist"][ok])
+    assert_same_cigars(cg, z["cigars"], np.flatnonzero(ok))
+    # the packing kernel against the reference's compact_sequences words
+    wps = z["packed"].shape[2] // 4
+    d_words = torch.full((n * 2 * wps,), -1, dtype=torch.int32, device="cuda")
+    wfe.pack_device(d_ascii, d_pairs, n, d_words, wps, torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    words = d_words.cpu().numpy().view(np.uint32).reshape(n, 2, wps)
+    np.testing.assert_array_equal(words, z["packed"].view("<u4").reshape(n, 2, wps))
+
+
+def test_golden_cigar_from_history(golden):
+    """The CIGAR kernel fed the reference's own 128-bit histories."""
+    torch = torch_cuda()
+    z, seqs, ascii, pairs = golden
+    n = len(seqs)
+    d_ascii = torch.from_numpy(ascii).cuda()
+    d_pairs = torch.from_numpy(pairs.view(np.uint8)).cuda()
+    d_dist = torch.from_numpy(z["dist"].astype(np.int32)).cuda()
+    d_hist = torch.from_numpy(z["words"].view(np.int64).reshape(-1)).cuda()
+    d_cg = torch.zeros(n * 152, dtype=torch.int8, device="cuda")
+    d_st = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    wfe.cigar_from_history_device(d_ascii, d_pairs, n, 300, d_dist, d_hist, d_cg, 152, d_st,
+                                  torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    cg = d_cg.cpu().numpy().reshape(n, 152)
+    st = d_st.cpu().numpy()
+    ok = z["dist"] < 64
+    assert (st[ok] == wfe.PAIR_OK).all()
+    assert_same_cigars(cg, z["cigars"], np.flatnonzero(ok))
+    assert (st[~ok] == wfe.PAIR_OVER_MAX_DISTANCE).all()
+
+
+# ---------------------------------------------------------------------------
+# synthetic workloads against the oracle
+
+@pytest.mark.parametrize("n,L,p,seed", [
+    (10000, 150, 0.02, 1),   # plain method, small
+    (100000, 150, 0.05, 2),  # one batch of the short-read throughput workload
+])
+def test_short_reads(n, L, p, seed):
+    ascii, pairs = wfe.generate(n, L, p_min=p, seed=seed)
+    with wfe.Context(max_seq_len=2 * L, cigar_stride=wfe.reference_cigar_stride(L)) as ctx:
+        dist, cg, st = ctx.align(ascii, pairs)
+    compare_with_oracle(ascii, pairs, wfe.reference_cigar_stride(L), dist, cg, st)
+
+
+def test_high_error_short_reads_cross_tiers():
+    """Distances from 0 to ~150 on 150-base reads exercise every tier
+    handing pairs on to the next."""
+    ascii, pairs = wfe.generate(6000, 150, p_min=0.0, p_max=0.9, seed=21)
+    with wfe.Context(max_seq_len=300, cigar_stride=600) as ctx:
+        dist, cg, st = ctx.align(ascii, pairs)
+    assert dist.max() > 143
+    compare_with_oracle(ascii, pairs, 600, dist, cg, st)
+
+
+def test_long_reads_sample():
+    ascii, pairs = wfe.generate(1500, 1000, p_min=0.10, seed=3)
+    with wfe.Context(max_seq_len=2000, cigar_stride=1004) as ctx:
+        dist, cg, st = ctx.align(ascii, pairs)
+    assert dist.mean() > 64
+    compare_with_oracle(ascii, pairs, 1004, dist, cg, st)
+
+
+def test_mixed_lengths_sample():
+    ascii, pairs = wfe.generate(1500, 100, 1500, p_min=0.01, p_max=0.15, seed=4)
+    with wfe.Context(max_seq_len=3000, cigar_stride=3004) as ctx:
+        dist, cg, st = ctx.align(ascii, pairs)
+    compare_with_oracle(ascii, pairs, 3004, dist, cg, st)
+
+
+def test_edge_cases():
+    seqs = [(b"", b""), (b"A", b""), (b"", b"ACGT"), (b"ACGT", b"ACGT"), (b"A" * 40, b"C" * 40),
+            (b"ACGTN", b"ACGTG"), (b"acgt", b"ACGT"), (b"A" * 299, b"A" * 300), (b"T" * 300, b""),
+            (b"G" * 16, b"G" * 16), (b"G" * 17, b"G" * 15), (b"ACGT" * 75, b"TGCA" * 75)]
+    for L in range(1, 40):
+        seqs.append((bytes(b"ACGT"[(i * 7 + L) % 4] for i in range(L)), bytes(b"ACGT"[(i * 5) % 4] for i in range(L))))
+    ascii, pairs = wfe.pairs_from_list(seqs)
+    with wfe.Context(max_seq_len=300, cigar_stride=604) as ctx:
+        dist, cg, st = ctx.align(ascii, pairs)
+    compare_with_oracle(ascii, pairs, 604, dist, cg, st)
+    assert dist[0] == 0 and cg[0, 0] == 0
+    assert dist[2] == 4 and wfe.format_cigar(cg[2]) == "4I"
+
+
+def test_unaligned_offsets_and_batches():
+    """Sequences at every byte alignment, several batches, both pipeline stages."""
+    ascii, pairs = wfe.generate(3000, 150, p_min=0.05, seed=8)
+    shifted = np.zeros(len(ascii) + 64, np.uint8)
+    shifted[7:7 + len(ascii)] = ascii
+    pairs2 = pairs.copy()
+    pairs2["p_off"] += 7
+    pairs2["t_off"] += 7
+    with wfe.Context(max_seq_len=300, batch_size=512) as ctx:
+        d1, c1, s1 = ctx.align(ascii, pairs)
+        d2, c2, s2 = ctx.align(shifted, pairs2)
+        assert ctx.stats()["batches"] == 12
+    np.testing.assert_array_equal(d1, d2)
+    assert_same_cigars(c1, c2)
+    compare_with_oracle(ascii, pairs, 152, d1, c1, s1)
+
+
+def test_scattered_pairs_gather_path():
+    """Pairs that point all over a large buffer go through the pinned gather."""
+    ascii, pairs = wfe.generate(2000, 150, p_min=0.05, seed=9)
+    perm = np.random.default_rng(0).permutation(len(pairs))
+    big = np.zeros(len(ascii) * 300, np.uint8)
+    pairs2 = pairs.copy()
+    for j, i in enumerate(perm):
+        base = j * 150 * 300 // 2
+        big[base: base + pairs["p_len"][i]] = ascii[pairs["p_off"][i]: pairs["p_off"][i] + pairs["p_len"][i]]
+        big[base + 320: base + 320 + pairs["t_len"][i]] = ascii[pairs["t_off"][i]: pairs["t_off"][i] + pairs["t_len"][i]]
+        pairs2[i]["p_off"], pairs2[i]["t_off"] = base, base + 320
+    with wfe.Context(max_seq_len=300, batch_size=700) as ctx:
+        d1, c1, s1 = ctx.align(ascii, pairs)
+        d2, c2, s2 = ctx.align(big, pairs2)
+    np.testing.assert_array_equal(d1, d2)
+    assert_same_cigars(c1, c2)
+
+
+def test_cigar_truncation_and_caps():
+    ascii, pairs = wfe.generate(500, 150, p_min=0.3, seed=12)
+    with wfe.Context(max_seq_len=300, cigar_stride=16) as ctx:
+        dist, cg, st = ctx.align(ascii, pairs)
+    compare_with_oracle(ascii, pairs, 16, dist, cg, st)
+    assert (st == wfe.PAIR_CIGAR_TRUNCATED).any()
+    with wfe.Context(max_seq_len=300, max_distance=20) as ctx:
+        dist, cg, st = ctx.align(ascii, pairs)
+    compare_with_oracle(ascii, pairs, 152, dist, cg, st, max_distance=20)
+    assert (st == wfe.PAIR_OVER_MAX_DISTANCE).any()
+
+
+def test_too_long_rejected():
+    ascii, pairs = wfe.generate(4, 200, p_min=0.05, seed=1)
+    with wfe.Context(max_seq_len=150) as ctx:
+        with pytest.raises(wfe.WfeError) as e:
+            ctx.align(ascii, pairs)
+    assert e.value.code == wfe.ERR_SEQ_TOO_LONG
+
+
+def test_full_short_read_workload_properties():
+    """All 1,000,000 pairs of the short-read workload: every CIGAR replays
+    against its pair and scores its distance; a 1-in-50 sample matches the
+    oracle byte for byte."""
+    ascii, pairs = wfe.generate(1000000, 150, p_min=0.05, seed=2)
+    with wfe.Context(max_seq_len=300, batch_size=100000) as ctx:
+        dist, cg, st = ctx.align(ascii, pairs)
+    assert (st == 0).all()
+    # replay: sum of M/X/D consumes the pattern, M/X/I the text, X+I+D = dist
+    # (only the bytes before each terminator count)
+    live = np.cumsum(cg == 0, axis=1) == 0
+    mruns = np.where(live & (cg < 0), -cg.astype(np.int64), 0).sum(1)
+    nx = (live & (cg == ord("X"))).sum(1)
+    ni = (live & (cg == ord("I"))).sum(1)
+    nd = (live & (cg == ord("D"))).sum(1)
+    np.testing.assert_array_equal(nx + ni + nd, dist)
+    np.testing.assert_array_equal(mruns + nx + nd, pairs["p_len"])
+    np.testing.assert_array_equal(mruns + nx + ni, pairs["t_len"])
+    sample = np.arange(0, len(pairs), 50)
+    sub_ascii, sub_pairs = ascii, pairs[sample]
+    od, ocg, ost, _ = oracle_run(sub_ascii, sub_pairs, 152)
+    np.testing.assert_array_equal(dist[sample], od)
+    assert_same_cigars(cg[sample], ocg)
