@@ -55,7 +55,32 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-batch", type=int, default=0,
+                    help="profiling case: align this many pairs of the workload as ONE batch, twice "
+                         "(a warm-up chain, then the chain to capture), and exit")
     return ap.parse_args()
+
+
+def run_profile_case(n: int) -> int:
+    """One batch of n pairs through wfe_align_device, twice.  For ncu: the
+    second chain's tier-0 launch is the 6th tier_kernel launch (-s 5 -c 1)."""
+    import torch
+    torch.cuda.set_device(0)
+    ascii, pairs = wfe.generate(n, LENGTH, p_min=EDIT_P, seed=SEED)
+    d_ascii = torch.from_numpy(ascii).cuda()
+    d_pairs = torch.from_numpy(pairs.view(np.uint8)).cuda()
+    d_dist = torch.zeros(n, dtype=torch.int32, device="cuda")
+    d_cigar = torch.zeros(n * CIGAR_STRIDE, dtype=torch.int8, device="cuda")
+    d_status = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    with wfe.Context(max_seq_len=MAX_SEQ_LEN, batch_size=n, cigar_stride=CIGAR_STRIDE) as ctx:
+        for _ in range(2):
+            ctx.align_device(d_ascii, d_pairs, n, MAX_SEQ_LEN, d_dist, d_cigar, d_status)
+            torch.cuda.synchronize()
+        launches = ctx.stats()["tier_launches"][:5]
+    mb = (len(ascii) + n * (CIGAR_STRIDE + 29)) / 2**20
+    print(json.dumps({"profile_batch": n, "device_MiB": round(mb, 1), "tier_launches": launches,
+                      "status_ok": bool((d_status.cpu().numpy() == 0).all())}))
+    return 0
 
 
 def dist_env():
@@ -216,6 +241,8 @@ def run_reference(args):
 
 def main():
     args = parse()
+    if args.profile_batch:
+        return run_profile_case(args.profile_batch)
     if args.impl == "reference":
         return run_reference(args)
     import torch

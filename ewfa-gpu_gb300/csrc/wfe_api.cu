@@ -90,7 +90,7 @@ uint32_t default_cigar_stride(uint32_t max_seq_len)
  * 8-lane tier; long reads start where their distances usually are. */
 int default_first_tier(uint32_t max_len)
 {
-    if (max_len <= 400) return 0;
+    if (max_len <= 1200) return 0;
     if (max_len <= 2000) return 2;
     return 3;
 }
@@ -369,13 +369,20 @@ int align_host(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, in
 {
     const wfe_config& c = ctx->cfg;
     WFE_CUDA(ctx, cudaSetDevice(c.device));
-    const size_t B = c.batch_size;
+    size_t B = c.batch_size;
+    if (!job.pairs) {
+        /* strided slots may be wider than max_seq_len: fewer pairs per batch */
+        const size_t fit = (ctx->st[0].ascii_cap - 32u) / (2u * job.stride);
+        if (fit == 0) return WFE_ERR_SEQ_TOO_LONG;
+        B = std::min(B, fit);
+    }
     const int nstages = (c.flags & WFE_FLAG_NO_PIPELINE) ? 1 : kStages;
     size_t bi = 0;
-    for (size_t b0 = 0; b0 < n; b0 += B, ++bi) {
+    size_t nb = 0;
+    for (size_t b0 = 0; b0 < n; b0 += nb, ++bi) {
         Stage& st = ctx->st[bi % nstages];
         cudaStream_t s = st.stream;
-        const size_t nb = std::min(B, n - b0);
+        nb = std::min(B, n - b0);
         Layout L{};
         if (job.pairs) {
             const wfe_pair* P = job.pairs + b0;

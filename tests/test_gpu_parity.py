@@ -163,14 +163,16 @@ def test_short_reads(n, L, p, seed):
     compare_with_oracle(ascii, pairs, wfe.reference_cigar_stride(L), dist, cg, st)
 
 
-def test_high_error_short_reads_cross_tiers():
-    """Distances from 0 to ~150 on 150-base reads exercise every tier
-    handing pairs on to the next."""
-    ascii, pairs = wfe.generate(6000, 150, p_min=0.0, p_max=0.9, seed=21)
-    with wfe.Context(max_seq_len=300, cigar_stride=600) as ctx:
+def test_high_error_pairs_cross_every_tier():
+    """Distances from 0 to ~330 (lengths 100-600, edit probability up to
+    0.9) start in the 8-lane tier and are handed on through every tier."""
+    ascii, pairs = wfe.generate(6000, 100, 600, p_min=0.0, p_max=0.9, seed=21)
+    with wfe.Context(max_seq_len=1200, cigar_stride=2000) as ctx:
         dist, cg, st = ctx.align(ascii, pairs)
-    assert dist.max() > 143
-    compare_with_oracle(ascii, pairs, 600, dist, cg, st)
+        stats = ctx.stats()
+    assert dist.max() > 271
+    assert all(stats["tier_passed"][t] > 0 for t in range(4)), stats
+    compare_with_oracle(ascii, pairs, 2000, dist, cg, st)
 
 
 def test_long_reads_sample():
