@@ -31,8 +31,10 @@ assert PAIR_DTYPE.itemsize == 24
 SYMBOLS = [
     "wfe_create", "wfe_destroy", "wfe_strerror", "wfe_last_cuda_error", "wfe_get_stats",
     "wfe_reset_stats", "wfe_align", "wfe_align_strided", "wfe_align_device", "wfe_pack_device",
-    "wfe_cigar_from_history_device", "wfe_format_cigar", "wfe_check_cigar",
+    "wfe_cigar_from_history_device", "wfe_format_cigar", "wfe_check_cigar", "wfe_align_device_noalloc",
 ]
+NOALLOC_MAX_DISTANCE = 271
+NOALLOC_SCRATCH_BYTES = 16 << 20
 
 
 class WfeError(RuntimeError):
@@ -91,6 +93,7 @@ def load() -> C.CDLL:
     L.wfe_format_cigar.argtypes = [vp, sz, C.c_char_p, sz, C.c_int]
     L.wfe_format_cigar.restype = sz
     L.wfe_check_cigar.argtypes = [C.c_char_p, u32, C.c_char_p, u32, vp, sz, C.POINTER(i32)]
+    L.wfe_align_device_noalloc.argtypes = [vp, vp, sz, u32, i32, vp, vp, u32, vp, vp]
     for name in SYMBOLS:
         getattr(L, name)
     _lib = L
@@ -281,6 +284,18 @@ def cigar_from_history_device(d_ascii, d_pairs, n: int, max_len: int, d_dist, d_
     _check(load().wfe_cigar_from_history_device(_addr(d_ascii), _addr(d_pairs), n, max_len, _addr(d_dist),
                                                 _addr(d_history), _addr(d_cigar), cigar_stride,
                                                 _addr(d_status), s), "wfe_cigar_from_history_device")
+
+
+def align_device_noalloc(d_ascii, d_pairs, n: int, max_len: int, max_distance: int, d_dist, d_cigar,
+                         cigar_stride: int, d_status, stream=None) -> None:
+    """wfe_align_device_noalloc: device buffers in and out, no allocation and
+    no context, for callers that cannot allocate device memory; scratch is the
+    library's fixed 16 MiB device array shared by every call (calls must not
+    overlap on the GPU)."""
+    s = stream.cuda_stream if hasattr(stream, "cuda_stream") else (stream or 0)
+    _check(load().wfe_align_device_noalloc(_addr(d_ascii), _addr(d_pairs), n, max_len, max_distance,
+                                           _addr(d_dist), _addr(d_cigar), cigar_stride, _addr(d_status), s),
+           "wfe_align_device_noalloc")
 
 
 def format_cigar(cigar: np.ndarray, compat: bool = False) -> str:

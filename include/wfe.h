@@ -188,6 +188,44 @@ int wfe_cigar_from_history_device(const char* d_ascii, const wfe_pair* d_pairs,
                                   uint32_t cigar_stride, uint8_t* d_status,
                                   void* stream);
 
+/* ---- allocation-free alignment ------------------------------------------ */
+
+/* Largest max_distance wfe_align_device_noalloc accepts, and the size of the
+ * fixed device array that holds its scratch. */
+#define WFE_NOALLOC_MAX_DISTANCE 271
+#define WFE_NOALLOC_SCRATCH_BYTES (16u << 20)
+
+/* Align n pairs whose ASCII and descriptors are in DEVICE memory, results to
+ * DEVICE memory, without allocating anything: no cudaMalloc, no cudaFree, no
+ * context.  No counterpart in the reference.  It is for callers that cannot
+ * allocate device memory where they align: a plugin whose host application
+ * owns every device allocation through its own pool, a real-time loop that
+ * forbids allocation after start-up, code on a memory budget that another
+ * framework accounts for.
+ *
+ * Runs on the current device, enqueued on `stream` (a cudaStream_t, NULL =
+ * the legacy default stream).  Arguments as wfe_align_device; max_distance
+ * must be 1..WFE_NOALLOC_MAX_DISTANCE (the search is bounded because its
+ * backtrace store is a fixed array): pairs farther apart get
+ * WFE_PAIR_OVER_MAX_DISTANCE and distance max_distance + 1, exactly as
+ * wfe_align_device does with the same max_distance.  Results are identical
+ * to wfe_align_device's.  Returns WFE_ERR_INVALID_ARGUMENT for a
+ * max_distance out of range, WFE_ERR_SEQ_TOO_LONG when max_len and
+ * cigar_stride do not fit the kernel's shared memory.
+ *
+ * Scratch: a WFE_NOALLOC_SCRATCH_BYTES array in the library's device image,
+ * held by every GPU that loads the library until the process exits.  The
+ * first call on a device looks up that array's device address (set-up, once
+ * per device); make that first call outside any stream capture.  Every call
+ * shares the array and it keeps the last call's contents (nothing in it has
+ * to start at zero: each entry is written before it is read).  Calls that
+ * overlap on the GPU -- on two streams, or from two host threads -- race on
+ * the array and corrupt each other's results: issue them on one stream. */
+int wfe_align_device_noalloc(const char* d_ascii, const wfe_pair* d_pairs, size_t n,
+                             uint32_t max_len, int32_t max_distance, int32_t* d_dist,
+                             int8_t* d_cigar, uint32_t cigar_stride, uint8_t* d_status,
+                             void* stream);
+
 /* ---- host CIGAR utilities ---------------------------------------------- */
 
 /* Text of one encoded CIGAR.  compat = 0: run-length form, e.g.
