@@ -200,6 +200,32 @@ def cpu_baseline(ascii, pairs, nthreads):
             "sample": f"all {len(pairs):,} pairs of the workload, {nthreads} threads, {dt:.2f} s"}
 
 
+def reference_cuda_baseline():
+    """The reference's own CUDA kernels (src/kernels.cu compiled for sm_100,
+    as its `make SM=100 COMPUTE=100 all` does) through a restatement of its
+    batch loop, timed like its wfe.aligner (wall time from before allocation
+    to after the last batch), on the same workload: -n 1000000 -l 150
+    -b 100000, -t 1/2/4/8, best of 3 each.  None where the kernels were not
+    compiled (they need the reference sources)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    try:
+        oracle.build(ref=False)
+    except Exception:
+        return None
+    if not oracle.ref_cuda_available():
+        return None
+    runs = {}
+    for t in (1, 2, 4, 8):
+        rec = oracle.ref_cuda_run(PAIRS, LENGTH, EDIT_P, SEED, batch=BATCH, threads=t, reps=3)
+        runs[t] = rec["alignments_per_s"]
+    best_t = max(runs, key=runs.get)
+    return {"value": runs[best_t], "unit": "alignments/s", "threads": best_t,
+            "by_threads": {str(t): round(v) for t, v in runs.items()},
+            "kind": "reference src/kernels.cu (sm_100 cubin) + restated src/wavefront.cu batch loop, "
+                    "wall time as src/aligner.cu:198-233, best of 3"}
+
+
 def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
@@ -345,8 +371,10 @@ def main():
         raise SystemExit("host-buffer and device-buffer results differ")
 
     base = None
+    ref_cuda = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         base = cpu_baseline(ascii, pairs, os.cpu_count() or 1)
+        ref_cuda = reference_cuda_baseline()
 
     if rank == 0:
         line = {
@@ -363,6 +391,7 @@ def main():
                          "kernel": f"tier_kernel tier {top}", "alg_bytes_per_launch": alg_bytes,
                          "launch_ms": launch_ms},
             "cpu_baseline": base,
+            "ref_cuda": ref_cuda,
             "e2e": e2e,
             "gpu_launches": gpu_launches,
             "clocks": clocks.summary(),

@@ -28,14 +28,38 @@ OP_INS, OP_SUB, OP_DEL = 1, 2, 3
 PAIR_OK, PAIR_OVER_MAX, PAIR_CIGAR_TRUNCATED = 0, 1, 2
 
 
+REF_CUBIN = os.path.join(HERE, "_ref", "ref_kernels_sm100.cubin")
+REF_HARNESS = os.path.join(HERE, "_build", "ref_cuda_harness")
+
+
 def build(ref: bool | None = None) -> None:
-    """Compile the restatement (and, if the reference sources exist, the
-    reference-on-CPU library)."""
+    """Compile the restatement and the driver of the reference's GPU kernels;
+    where the reference sources exist, also the reference-on-CPU library and
+    the reference's kernels as an sm_100 cubin."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
     if ref is None:
         ref = os.path.isdir(os.path.join(REF_SRC, "src"))
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "ref-cubin", f"REF={REF_SRC}"], check=True)
+    if os.path.exists(REF_CUBIN):
+        subprocess.run(["make", "-s", "-C", HERE, "ref-harness"], check=False)
+
+
+def ref_cuda_available() -> bool:
+    return os.path.exists(REF_CUBIN) and os.path.exists(REF_HARNESS)
+
+
+def ref_cuda_run(n: int, length: int, p: float, seed: int, batch: int | None = None, threads: int = 1,
+                 reps: int = 1, dump: str | None = None) -> dict:
+    """Run the reference's own GPU kernels (sm_100 cubin) through the
+    restated batch loop; returns the harness's JSON record."""
+    import json
+    cmd = [REF_HARNESS, "--cubin", REF_CUBIN, "-n", str(n), "-l", str(length), "-b", str(batch or n),
+           "-t", str(threads), "--p", str(p), "--seed", str(seed), "--reps", str(reps)]
+    if dump:
+        cmd += ["--dump", dump]
+    out = subprocess.run(cmd, check=True, stdout=subprocess.PIPE, text=True).stdout
+    return json.loads(out.strip().splitlines()[-1])
 
 
 class _Counts(C.Structure):
