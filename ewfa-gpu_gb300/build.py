@@ -23,7 +23,9 @@ LIB = os.path.join(PKG, "lib")
 BIN = os.path.join(PKG, "bin")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
+# relocatable device code: the tier kernels launch their successors on the
+# device (tail launches), which needs the device runtime (cudadevrt)
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-rdc=true", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
               f"-I{INC}", f"-I{CSRC}"] + ARCH
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wextra", f"-I{INC}", f"-I{CSRC}"]
 CC_FLAGS = ["-O2", "-std=c11", "-fPIC", "-Wall", "-Wextra", "-ffp-contract=off", f"-I{INC}", f"-I{CSRC}"]
@@ -89,7 +91,7 @@ def build(verbose: bool = False) -> dict:
 
     libwfe = os.path.join(LIB, "libwfe.so")
     if _stale(libwfe, objs):
-        _run([nvcc] + ARCH + ["-shared", "-o", libwfe] + objs + ["-lpthread"])
+        _run([nvcc] + ARCH + ["-shared", "-rdc=true", "-o", libwfe] + objs + ["-lcudadevrt", "-lpthread"])
     libgen = os.path.join(LIB, "libwfe_gen.so")
     if _stale(libgen, [gen_obj]):
         _run(["gcc", "-shared", "-o", libgen, gen_obj, "-lm", "-lpthread"])

@@ -56,9 +56,11 @@ struct wfe_ctx {
     int sm_count = 0;
     int first_tier = 0;
     int grid[kNumTiers] = {};
+    TierShape shape[kNumTiers] = {};
     unsigned char* d_ops_scratch = nullptr;
     size_t ops_scratch_bytes = 0;
-    unsigned long long* d_passed = nullptr; /* pairs each tier handed on, running total */
+    unsigned long long* d_passed = nullptr;   /* pairs each tier handed on, running total */
+    unsigned long long* d_launched = nullptr; /* tier launches made on the device */
     Stage st[kStages];
     int last_cuda_error = 0;
     wfe_stats stats{};
@@ -112,71 +114,71 @@ void free_stage(Stage& s)
     s = Stage();
 }
 
-/* Enqueue the tier chain for work items 0..n-1 of one batch on stream s. */
+/* Enqueue the alignment of work items 0..n-1 of one batch on stream s: the
+ * first tier is launched here; each tier's last CTA launches the next tier
+ * on the device, and only when it handed pairs on. */
 int run_chain(wfe_ctx* ctx, Stage& st, const Layout& L, uint32_t n, int32_t* dist, int8_t* cigar,
               uint8_t* status, cudaStream_t s)
 {
     if (n == 0) return WFE_OK;
     const wfe_config& c = ctx->cfg;
-    WFE_CUDA(ctx, cudaMemsetAsync(st.d_counts, 0, sizeof(uint32_t) * kNumTiers, s));
+    WFE_CUDA(ctx, cudaMemsetAsync(st.d_counts, 0, sizeof(uint32_t) * 2 * kNumTiers, s));
     const uint32_t B = c.batch_size;
-    for (int t = ctx->first_tier; t < kNumTiers; ++t) {
-        AlignLaunch a{};
-        a.L = L;
-        const int k = t - ctx->first_tier;
-        if (k == 0) {
-            a.work = nullptr;
-            a.work_count = nullptr;
-            a.n_work = n;
-        } else {
-            a.work = st.d_lists + (size_t)((k - 1) & 1) * B;
-            a.work_count = st.d_counts + (t - 1);
-            a.n_work = n;
-        }
-        a.dist = dist;
-        a.cigar = cigar;
-        a.cigar_stride = c.cigar_stride;
-        a.status = status;
-        a.max_distance = c.max_distance;
-        a.max_len = c.max_seq_len;
-        a.retry = (t + 1 < kNumTiers) ? st.d_lists + (size_t)(k & 1) * B : nullptr;
-        a.retry_count = st.d_counts + t;
-        a.ops_scratch = ctx->d_ops_scratch;
-        a.ops_scratch_bytes = ctx->ops_scratch_bytes;
-        /* the first tier is sized to the batch; later tiers run persistent
-         * grids that read their work count on the device */
-        int grid = ctx->grid[t];
-        if (k == 0) {
-            const TierInfo& ti = tier_info(t);
-            const uint32_t per_cta = 4u * (32u / (uint32_t)ti.G);
-            grid = (int)std::min<uint64_t>((uint64_t)grid, ((uint64_t)n + per_cta - 1) / per_cta);
-            grid = std::max(grid, 1);
-        }
-        a.passed_total = ctx->d_passed + t;
-        TimedLaunch tl{t, nullptr, nullptr};
-        const bool timing = (c.flags & WFE_FLAG_KERNEL_TIMING) != 0;
-        if (timing) {
-            for (cudaEvent_t* ev : {&tl.start, &tl.stop}) {
-                if (!ctx->event_pool.empty()) {
-                    *ev = ctx->event_pool.back();
-                    ctx->event_pool.pop_back();
-                } else {
-                    WFE_CUDA(ctx, cudaEventCreate(ev));
-                }
+    const int t = ctx->first_tier;
+    AlignLaunch a{};
+    a.L = L;
+    a.work = nullptr;
+    a.work_count = nullptr;
+    a.n_work = n;
+    a.dist = dist;
+    a.cigar = cigar;
+    a.cigar_stride = c.cigar_stride;
+    a.status = status;
+    a.max_distance = c.max_distance;
+    a.max_len = c.max_seq_len;
+    a.retry = (t + 1 < kNumTiers) ? st.d_lists : nullptr;
+    a.retry_count = st.d_counts + t;
+    a.passed_total = ctx->d_passed + t;
+    a.ops_scratch = ctx->d_ops_scratch;
+    a.ops_scratch_bytes = ctx->ops_scratch_bytes;
+    a.tier = t;
+    /* a distance cap at or below a tier's capacity ends the chain there */
+    int last = kNumTiers - 1;
+    if (c.max_distance > 0)
+        for (int u = t; u < kNumTiers; ++u)
+            if (c.max_distance <= tier_info(u).dcap) { last = u; break; }
+    a.chain.last_tier = last;
+    for (int u = 0; u < kNumTiers; ++u) a.chain.shape[u] = ctx->shape[u];
+    a.chain.lists[0] = st.d_lists;
+    a.chain.lists[1] = st.d_lists + B;
+    a.chain.counts = st.d_counts;
+    a.chain.cta_done = st.d_counts + kNumTiers;
+    a.chain.launched = ctx->d_launched;
+    const TierInfo& ti = tier_info(t);
+    const uint32_t per_cta = 4u * (32u / (uint32_t)ti.G);
+    int grid = (int)std::min<uint64_t>((uint64_t)ctx->grid[t], ((uint64_t)n + per_cta - 1) / per_cta);
+    grid = std::max(grid, 1);
+    TimedLaunch tl{t, nullptr, nullptr};
+    const bool timing = (c.flags & WFE_FLAG_KERNEL_TIMING) != 0;
+    if (timing) {
+        for (cudaEvent_t* ev : {&tl.start, &tl.stop}) {
+            if (!ctx->event_pool.empty()) {
+                *ev = ctx->event_pool.back();
+                ctx->event_pool.pop_back();
+            } else {
+                WFE_CUDA(ctx, cudaEventCreate(ev));
             }
-            WFE_CUDA(ctx, cudaEventRecord(tl.start, s));
         }
-        WFE_CUDA(ctx, launch_tier(t, a, grid, s));
-        if (timing) {
-            WFE_CUDA(ctx, cudaEventRecord(tl.stop, s));
-            ctx->timed.push_back(tl);
-        }
-        ctx->stats.kernel_launches++;
-        ctx->stats.tier_launches[t]++;
-        if (k == 0) ctx->stats.tier_entered[t] += n;
-        /* a distance cap below the tier's capacity ends the chain */
-        if (c.max_distance > 0 && c.max_distance <= tier_info(t).dcap) break;
+        WFE_CUDA(ctx, cudaEventRecord(tl.start, s));
     }
+    WFE_CUDA(ctx, launch_tier(t, a, grid, s));
+    if (timing) {
+        WFE_CUDA(ctx, cudaEventRecord(tl.stop, s));
+        ctx->timed.push_back(tl);
+    }
+    ctx->stats.kernel_launches++;
+    ctx->stats.tier_launches[t]++;
+    ctx->stats.tier_entered[t] += n;
     return WFE_OK;
 }
 
@@ -239,7 +241,8 @@ int wfe_create(const wfe_config* cfg, wfe_ctx** out)
     if (e != cudaSuccess) return bail(e);
     size_t scratch = 0;
     for (int t = 0; t < kNumTiers; ++t) {
-        ctx->grid[t] = tier_grid(t, c.max_seq_len, c.cigar_stride, ctx->sm_count);
+        ctx->shape[t] = tier_shape(t, c.max_seq_len, c.cigar_stride, ctx->sm_count);
+        ctx->grid[t] = ctx->shape[t].grid;
         if (ctx->grid[t] <= 0) { /* sequences too long for this tier's shared memory */
             if (t >= ctx->first_tier) return bail(cudaErrorInvalidValue);
             continue;
@@ -251,8 +254,9 @@ int wfe_create(const wfe_config* cfg, wfe_ctx** out)
         if (e != cudaSuccess) return bail(e);
         ctx->ops_scratch_bytes = scratch;
     }
-    if ((e = cudaMalloc(&ctx->d_passed, sizeof(unsigned long long) * kNumTiers)) != cudaSuccess) return bail(e);
-    if ((e = cudaMemset(ctx->d_passed, 0, sizeof(unsigned long long) * kNumTiers)) != cudaSuccess) return bail(e);
+    if ((e = cudaMalloc(&ctx->d_passed, sizeof(unsigned long long) * 2 * kNumTiers)) != cudaSuccess) return bail(e);
+    if ((e = cudaMemset(ctx->d_passed, 0, sizeof(unsigned long long) * 2 * kNumTiers)) != cudaSuccess) return bail(e);
+    ctx->d_launched = ctx->d_passed + kNumTiers;
     const size_t B = c.batch_size;
     for (auto& s : ctx->st) {
         s.ascii_cap = B * 2u * (size_t)c.max_seq_len + 64u;
@@ -265,7 +269,7 @@ int wfe_create(const wfe_config* cfg, wfe_ctx** out)
         if ((e = cudaMalloc(&s.d_cigar, B * (size_t)c.cigar_stride + 16u)) != cudaSuccess) return bail(e);
         if ((e = cudaMalloc(&s.d_status, B)) != cudaSuccess) return bail(e);
         if ((e = cudaMalloc(&s.d_lists, 2u * B * sizeof(uint32_t))) != cudaSuccess) return bail(e);
-        if ((e = cudaMalloc(&s.d_counts, sizeof(uint32_t) * kNumTiers)) != cudaSuccess) return bail(e);
+        if ((e = cudaMalloc(&s.d_counts, sizeof(uint32_t) * 2 * kNumTiers)) != cudaSuccess) return bail(e);
     }
     *out = ctx;
     return WFE_OK;
@@ -303,12 +307,14 @@ int wfe_get_stats(wfe_ctx* ctx, wfe_stats* out)
         ctx->event_pool.push_back(t.stop);
     }
     ctx->timed.clear();
-    unsigned long long passed[kNumTiers] = {};
-    WFE_CUDA(ctx, cudaMemcpy(passed, ctx->d_passed, sizeof(passed), cudaMemcpyDeviceToHost));
+    unsigned long long dev[2 * kNumTiers] = {};
+    WFE_CUDA(ctx, cudaMemcpy(dev, ctx->d_passed, sizeof(dev), cudaMemcpyDeviceToHost));
     *out = ctx->stats;
     for (int t = 0; t < kNumTiers; ++t) {
-        out->tier_passed[t] = passed[t];
-        if (t > ctx->first_tier) out->tier_entered[t] = passed[t - 1];
+        out->tier_passed[t] = dev[t];
+        if (t > ctx->first_tier) out->tier_entered[t] = dev[t - 1];
+        out->tier_launches[t] += dev[kNumTiers + t];
+        out->kernel_launches += dev[kNumTiers + t];
     }
     return WFE_OK;
 }
@@ -320,7 +326,7 @@ int wfe_reset_stats(wfe_ctx* ctx)
     const int r = wfe_get_stats(ctx, &tmp); /* drains pending timings */
     if (r != WFE_OK) return r;
     ctx->stats = wfe_stats{};
-    WFE_CUDA(ctx, cudaMemset(ctx->d_passed, 0, sizeof(unsigned long long) * kNumTiers));
+    WFE_CUDA(ctx, cudaMemset(ctx->d_passed, 0, sizeof(unsigned long long) * 2 * kNumTiers));
     return WFE_OK;
 }
 

@@ -108,21 +108,56 @@ __device__ __forceinline__ uint32_t packed_word(const char* s, uint32_t len,
 }
 
 /* Pack a sequence into overlapped pairs Q[0..nw) (see top of file) by a
- * group of G lanes; Q[nw-1].x = 0.  The caller syncs the group afterwards. */
-template <int G>
+ * group of G lanes; Q[nw-1].x = 0.  When the sequence spans at most RMAX*G
+ * aligned blocks, every lane issues all of its block loads first (blocks g,
+ * g+G, ...) and the neighbour block for the funnel shift comes from one
+ * rotating shuffle per word; longer sequences take the word-by-word loop.
+ * The caller syncs the group afterwards. */
+template <int G, int RMAX>
 __device__ __forceinline__ void load_packed(const char* s, uint32_t len, uint2* Q,
                                             int g, unsigned mask)
 {
     const uint32_t nw = (len + 15u) >> 4;
-    for (uint32_t w0 = 0; w0 < nw; w0 += G) {
-        const uint32_t W = packed_word<G>(s, len, w0, g, mask);
-        const uint32_t w = w0 + (uint32_t)g;
-        if (w < nw) {
-            Q[w].y = W;
-            if (w > 0) Q[w - 1].x = W;
+    if (nw == 0) return;
+    const uintptr_t a = reinterpret_cast<uintptr_t>(s);
+    const uint32_t sh = (uint32_t)(a & 15u);
+    const uint4* base = reinterpret_cast<const uint4*>(a - sh);
+    const uint32_t nblk = (sh + len + 15u) >> 4;
+    if (nblk <= (uint32_t)(RMAX * G)) {
+        uint32_t x[RMAX + 1];
+#pragma unroll
+        for (int r = 0; r < RMAX; ++r) {
+            const uint32_t b = (uint32_t)(g + r * G);
+            x[r] = b < nblk ? pack16(__ldg(base + b)) : 0u;
+        }
+        x[RMAX] = 0u;
+#pragma unroll
+        for (int r = 0; r < RMAX; ++r) {
+            if ((uint32_t)(r * G) >= nw) break;
+            /* block w+1 is lane g+1's block r, or lane 0's block r+1 for the
+             * last lane */
+            const uint32_t y = (g == 0) ? x[r + 1] : x[r];
+            const uint32_t nb = __shfl_sync(mask, y, (g + 1) & (G - 1), G);
+            const uint32_t w = (uint32_t)(g + r * G);
+            uint32_t W = sh ? __funnelshift_l(nb, x[r], 2u * sh) : x[r];
+            if (w < nw) {
+                const uint32_t rem = len - 16u * w;
+                if (rem < 16u) W &= ~0u << (2u * (16u - rem));
+                Q[w].y = W;
+                if (w > 0) Q[w - 1].x = W;
+            }
+        }
+    } else {
+        for (uint32_t w0 = 0; w0 < nw; w0 += G) {
+            const uint32_t W = packed_word<G>(s, len, w0, g, mask);
+            const uint32_t w = w0 + (uint32_t)g;
+            if (w < nw) {
+                Q[w].y = W;
+                if (w > 0) Q[w - 1].x = W;
+            }
         }
     }
-    if (g == 0 && nw > 0) Q[nw - 1].x = 0u;
+    if (g == 0) Q[nw - 1].x = 0u;
 }
 
 /* 16-base window of a packed sequence starting at base v. */
@@ -181,46 +216,36 @@ __device__ __forceinline__ int group_extend(const uint2* QP, const uint2* QT, in
     }
 }
 
-/* Byte writer into a CIGAR staging buffer of `cap` bytes (src/kernels.cu:
- * 437-446 run chunks, 456-470 operation letters). */
-struct CigarSink {
-    int8_t* buf;
-    uint32_t cap;
-    uint32_t pos;
-    __device__ __forceinline__ void put(int8_t b)
-    {
-        if (pos < cap) buf[pos] = b;
-        ++pos;
-    }
-    __device__ __forceinline__ void run(int n)
-    {
-        for (int j = 0; j < n / 127; ++j) put((int8_t)-127);
-        if (n % 127) put((int8_t)(-(n % 127)));
-    }
-};
-
 __device__ __forceinline__ int8_t op_letter(int op)
 {
     return op == kOpDel ? (int8_t)'D' : (op == kOpSub ? (int8_t)'X' : (int8_t)'I');
 }
 
-/* Forward replay of an operation chain (src/kernels.cu:397-498) by a group:
- * extend from (k=0, off=0), emit the run, apply op d, ..., final extend.
- * chain[d] is the operation of score d+1.  Lane 0 writes the bytes into
- * sink.  Returns the full CIGAR length (on every lane), or a negative value
- * if the chain holds a code other than INS/SUB/DEL (stops there, like the
- * reference's "Incorrect backtrace" exit, src/kernels.cu:471-478). */
+/* Forward replay of an operation chain into an encoded CIGAR
+ * (src/kernels.cu:397-498) by a group of G lanes.  chain[d] is the operation
+ * of score d+1.
+ *   1. In order of d, the run of M bases before operation d comes from a
+ *      group-parallel extend from (k, off), starting at (0, 0); runs[d]
+ *      keeps it (lane 0 writes).
+ *   2. In parallel, lane g takes steps g, g+G, ...: each step's bytes are its
+ *      run as chunks of at most 127 (-127, ..., -(run % 127)) and then its
+ *      operation letter; an inclusive shuffle scan over the group gives the
+ *      step's first byte, and every lane writes its own bytes into buf (cap
+ *      bytes; positions past cap are counted but not written).
+ * Returns the full CIGAR length on every lane, or -1 - length if the chain
+ * holds a code other than INS/SUB/DEL: the CIGAR then stops after that
+ * step's run, like the reference's "Incorrect backtrace" exit
+ * (src/kernels.cu:471-478). */
 template <int G>
 __device__ __forceinline__ int replay_chain(const uint2* QP, const uint2* QT, int plen, int tlen,
-                                            const uint8_t* chain, int D, CigarSink& sink,
-                                            int g, int grp, unsigned gmask)
+                                            const uint8_t* chain, int D, int* runs, int8_t* buf,
+                                            uint32_t cap, int g, int grp, unsigned gmask)
 {
-    int k = 0, off = 0;
-    int bad = 0;
+    int k = 0, off = 0, bad_at = -1;
     for (int d = 0; d <= D; ++d) {
         const int run = group_extend<G>(QP, QT, plen, tlen, k, off, g, grp, gmask);
+        if (g == 0) runs[d] = run;
         off += run;
-        if (g == 0) sink.run(run);
         if (d == D) break;
         const int op = chain[d];
         if (op == kOpDel) {
@@ -231,13 +256,45 @@ __device__ __forceinline__ int replay_chain(const uint2* QP, const uint2* QT, in
             ++k;
             ++off;
         } else {
-            bad = 1;
+            bad_at = d;
             break;
         }
-        if (g == 0) sink.put(op_letter(op));
     }
-    const int pos = (int)__shfl_sync(gmask, sink.pos, 0, G);
-    return bad ? -1 - pos : pos;
+    const int last = bad_at >= 0 ? bad_at : D;
+    __syncwarp(gmask);
+    int total = 0;
+    for (int base = 0; base <= last; base += G) {
+        const int d = base + g;
+        int r = 0, letter = 0, nb = 0;
+        if (d <= last) {
+            r = runs[d];
+            letter = (d < D && d != bad_at) ? (int)op_letter(chain[d]) : 0;
+            nb = r / 127 + (r % 127 != 0) + (letter != 0);
+        }
+        int x = nb;
+#pragma unroll
+        for (int sft = 1; sft < G; sft <<= 1) {
+            const int y = __shfl_up_sync(gmask, x, sft, G);
+            if (g >= sft) x += y;
+        }
+        uint32_t pos = (uint32_t)(total + x - nb);
+        if (d <= last) {
+            for (int j = 0; j < r / 127; ++j) {
+                if (pos < cap) buf[pos] = (int8_t)-127;
+                ++pos;
+            }
+            if (r % 127) {
+                if (pos < cap) buf[pos] = (int8_t)(-(r % 127));
+                ++pos;
+            }
+            if (letter) {
+                if (pos < cap) buf[pos] = (int8_t)letter;
+                ++pos;
+            }
+        }
+        total += __shfl_sync(gmask, x, G - 1, G);
+    }
+    return bad_at >= 0 ? -1 - total : total;
 }
 
 /* Copy a staged CIGAR of `len` bytes (plus terminator when it fits) from

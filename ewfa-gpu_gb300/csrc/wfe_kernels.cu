@@ -2,7 +2,7 @@
  * wfe_kernels.cu -- the alignment path on sm_103a.
  *
  *   pack_kernel          ASCII -> 2-bit words (src/kernels.cu:313-394)
- *   tier_kernel<G,J,S>   fused load+pack, wavefront compute+extend, bit-packed
+ *   tier_kernel<Tier>    fused load+pack, wavefront compute+extend, bit-packed
  *                        backtrace store, backtrace and CIGAR replay for one
  *                        pair per group of G lanes (src/kernels.cu:27-310 and
  *                        397-625 in one kernel)
@@ -40,6 +40,13 @@ __host__ __device__ constexpr size_t round16(size_t x) { return (x + 15u) & ~siz
 /* 2 bits per diagonal for the G diagonals of one chunk: the low bits of the
  * operations, then the high bits. */
 template <int G> struct OpEntry;
+template <> struct OpEntry<4> {
+    using T = uint8_t;
+    static __device__ __forceinline__ void put(T* p, int i, uint32_t lo, uint32_t hi)
+    { p[i] = (T)(lo | (hi << 4)); }
+    static __device__ __forceinline__ int get(const T* p, int i, int gl)
+    { const uint32_t e = p[i]; return (int)(((e >> gl) & 1u) | (((e >> (4 + gl)) & 1u) << 1)); }
+};
 template <> struct OpEntry<8> {
     using T = uint16_t;
     static __device__ __forceinline__ void put(T* p, int i, uint32_t lo, uint32_t hi)
@@ -62,9 +69,13 @@ template <> struct OpEntry<32> {
     { const uint2 e = p[i]; return (int)(((e.x >> gl) & 1u) | (((e.y >> gl) & 1u) << 1)); }
 };
 
-template <int G_, int J_, bool SMEM_OPS_>
+/* One distance tier: G lanes per pair, 2J+1 register chunks, backtrace
+ * store in shared (SMEM_OPS) or global memory, sequences of up to RMAX*G
+ * aligned 16-byte blocks loaded with all loads in flight at once, at least
+ * MINB resident CTAs per SM asked of the register allocator. */
+template <int G_, int J_, bool SMEM_OPS_, int RMAX_, int MINB_ = 1>
 struct Tier {
-    static constexpr int G = G_, J = J_;
+    static constexpr int G = G_, J = J_, RMAX = RMAX_, MINB = MINB_;
     static constexpr bool SMEM_OPS = SMEM_OPS_;
     static constexpr int NC = 2 * J + 1;
     static constexpr int DCAP = G * J + G / 2 - 1;
@@ -73,15 +84,26 @@ struct Tier {
     using E = typename OE::T;
     static constexpr size_t ops_bytes = round16(sizeof(E) * (size_t)DCAP * NC);
     static constexpr size_t chain_bytes = round16((size_t)DCAP + 1);
+    static constexpr size_t runs_bytes = round16(sizeof(int) * ((size_t)DCAP + 1));
 };
 
 inline uint32_t seq_words_for(uint32_t max_len) { return std::max<uint32_t>(1u, (max_len + 15u) / 16u); }
 
+/* Shared memory of one group: both sequences, the operation chain, then one
+ * region that first holds the backtrace store (when it lives in shared
+ * memory) and, once the chain has been read from it, the CIGAR stage and the
+ * runs of the replay. */
+template <class T>
+size_t union_bytes(uint32_t cigar_stride)
+{
+    const size_t replay = round16(cigar_stride) + T::runs_bytes;
+    return T::SMEM_OPS ? std::max(T::ops_bytes, replay) : replay;
+}
+
 template <class T>
 size_t group_smem_bytes(uint32_t max_len, uint32_t cigar_stride)
 {
-    return 16u * (size_t)seq_words_for(max_len) + (T::SMEM_OPS ? T::ops_bytes : 0u) +
-           T::chain_bytes + round16(cigar_stride);
+    return 16u * (size_t)seq_words_for(max_len) + T::chain_bytes + union_bytes<T>(cigar_stride);
 }
 
 template <class T>
@@ -91,7 +113,56 @@ size_t cta_smem_bytes(uint32_t max_len, uint32_t cigar_stride)
 }
 
 template <class T>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, T::MINB)
+tier_kernel(AlignLaunch A, uint32_t seq_words, uint32_t gbytes);
+
+/* Tier 0 carries the short-read workloads; its shape is tuned on the GPU
+ * (4 lanes per pair, 11 chunks, 8 resident CTAs per SM by default). */
+#ifndef WFE_T0_J
+#define WFE_T0_J 5
+#endif
+#ifndef WFE_T0_MINB
+#define WFE_T0_MINB 8
+#endif
+using T0 = Tier<4, WFE_T0_J, true, 5, WFE_T0_MINB>; /* distance <= 4*J + 1 (21) */
+using T1 = Tier<32, 2, true, 1>;   /* distance <= 79  */
+using T2 = Tier<32, 4, true, 1>;   /* distance <= 143 */
+using T3 = Tier<32, 8, false, 1>;  /* distance <= 271 */
+using T4 = Tier<32, 16, false, 1>; /* distance <= 527 */
+
+template <class T>
+__device__ void launch_on_device(const AlignLaunch& a, uint32_t count)
+{
+    const TierShape& sh = a.chain.shape[a.tier];
+    const uint32_t per_cta = (uint32_t)(kWarps * T::GPW);
+    const int grid = max(1, min(sh.grid, (int)((count + per_cta - 1u) / per_cta)));
+    tier_kernel<T><<<grid, kThreads, sh.smem, cudaStreamTailLaunch>>>(a, sh.seq_words, sh.gbytes);
+    if (a.chain.launched) atomicAdd(a.chain.launched + a.tier, 1ull);
+}
+
+/* Called by the last CTA of tier A.tier when it handed `count` pairs on:
+ * the next tier runs over them once this grid has completed. */
+__device__ __noinline__ void launch_next_tier(const AlignLaunch& A, uint32_t count)
+{
+    AlignLaunch n = A;
+    n.tier = A.tier + 1;
+    n.work = A.retry;
+    n.work_count = A.retry_count;
+    n.retry = n.tier + 1 < kNumTiers ? (A.retry == A.chain.lists[0] ? A.chain.lists[1] : A.chain.lists[0])
+                                     : nullptr;
+    n.retry_count = A.chain.counts + n.tier;
+    n.passed_total = A.passed_total ? A.passed_total + 1 : nullptr;
+    switch (n.tier) {
+    case 1: launch_on_device<T1>(n, count); break;
+    case 2: launch_on_device<T2>(n, count); break;
+    case 3: launch_on_device<T3>(n, count); break;
+    case 4: launch_on_device<T4>(n, count); break;
+    default: break;
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kThreads, T::MINB)
 tier_kernel(AlignLaunch A, uint32_t seq_words, uint32_t gbytes)
 {
     constexpr int G = T::G, J = T::J, NC = T::NC, DCAP = T::DCAP, GPW = T::GPW;
@@ -108,18 +179,17 @@ tier_kernel(AlignLaunch A, uint32_t seq_words, uint32_t gbytes)
     unsigned char* gs = smem + (size_t)slot * gbytes;
     uint2* QP = reinterpret_cast<uint2*>(gs);
     uint2* QT = QP + seq_words;
-    unsigned char* cur = gs + 16u * (size_t)seq_words;
+    uint8_t* chain = gs + 16u * (size_t)seq_words;
+    unsigned char* uni = chain + T::chain_bytes;
     E* ops;
     if constexpr (T::SMEM_OPS) {
-        ops = reinterpret_cast<E*>(cur);
-        cur += T::ops_bytes;
+        ops = reinterpret_cast<E*>(uni);
     } else {
         const size_t gslot = (size_t)blockIdx.x * (kWarps * GPW) + (size_t)slot;
         ops = reinterpret_cast<E*>(A.ops_scratch + gslot * T::ops_bytes);
     }
-    uint8_t* chain = cur;
-    cur += T::chain_bytes;
-    int8_t* stage = reinterpret_cast<int8_t*>(cur);
+    int8_t* stage = reinterpret_cast<int8_t*>(uni);
+    int* runs = reinterpret_cast<int*>(uni + round16(A.cigar_stride));
 
     const uint32_t count = A.work_count ? min(*A.work_count, A.n_work) : A.n_work;
     const uint32_t step = gridDim.x * (uint32_t)(kWarps * GPW);
@@ -137,8 +207,8 @@ tier_kernel(AlignLaunch A, uint32_t seq_words, uint32_t gbytes)
         }
         const uint32_t lp = state == ST_RUN ? pr.plen : 0u;
         const uint32_t lt = state == ST_RUN ? pr.tlen : 0u;
-        load_packed<G>(pr.p, lp, QP, g, gmask);
-        load_packed<G>(pr.t, lt, QT, g, gmask);
+        load_packed<G, T::RMAX>(pr.p, lp, QP, g, gmask);
+        load_packed<G, T::RMAX>(pr.t, lt, QT, g, gmask);
         __syncwarp();
 
         const int plen = (int)lp, tlen = (int)lt, kt = tlen - plen;
@@ -225,8 +295,8 @@ tier_kernel(AlignLaunch A, uint32_t seq_words, uint32_t gbytes)
         }
         if (state == ST_DONE) {
             __syncwarp(gmask);
-            CigarSink sink{stage, A.cigar_stride, 0u};
-            const int len = replay_chain<G>(QP, QT, plen, tlen, chain, D, sink, g, grp, gmask);
+            const int len = replay_chain<G>(QP, QT, plen, tlen, chain, D, runs, stage, A.cigar_stride,
+                                            g, grp, gmask);
             if (A.cigar_stride)
                 store_cigar<G>(stage, (uint32_t)len, A.cigar_stride,
                                A.cigar + (size_t)pi * A.cigar_stride, g, gmask);
@@ -256,13 +326,21 @@ tier_kernel(AlignLaunch A, uint32_t seq_words, uint32_t gbytes)
         }
         __syncwarp();
     }
-}
 
-using T0 = Tier<8, 3, true>;    /* distance <= 27  */
-using T1 = Tier<32, 2, true>;   /* distance <= 79  */
-using T2 = Tier<32, 4, true>;   /* distance <= 143 */
-using T3 = Tier<32, 8, false>;  /* distance <= 271 */
-using T4 = Tier<32, 16, false>; /* distance <= 527 */
+    /* the last CTA to finish starts the next tier if this one handed pairs on */
+    if (A.chain.cta_done) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            const unsigned t = atomicAdd(A.chain.cta_done + A.tier, 1u);
+            if (t == gridDim.x - 1u) {
+                __threadfence();
+                const uint32_t cnt = *reinterpret_cast<volatile const uint32_t*>(A.retry_count);
+                if (cnt > 0u && A.tier < A.chain.last_tier) launch_next_tier(A, cnt);
+            }
+        }
+    }
+}
 
 const TierInfo kTiers[kNumTiers] = {
     {T0::G, T0::J, T0::DCAP, T0::SMEM_OPS},
@@ -273,15 +351,27 @@ const TierInfo kTiers[kNumTiers] = {
 };
 
 template <class T>
-int grid_of(uint32_t max_len, uint32_t cigar_stride, int sm_count)
+TierShape shape_of(uint32_t max_len, uint32_t cigar_stride, int sm_count)
 {
+    TierShape sh{};
     const size_t smem = cta_smem_bytes<T>(max_len, cigar_stride);
-    if (smem > 227u * 1024u) return 0;
-    cudaFuncSetAttribute(tier_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (smem > 227u * 1024u) return sh;
+    if (cudaFuncSetAttribute(tier_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return sh;
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, tier_kernel<T>, kThreads, smem) != cudaSuccess)
-        return 0;
-    return std::max(1, nb) * sm_count;
+        return sh;
+    sh.grid = std::max(1, nb) * sm_count;
+    sh.smem = (uint32_t)smem;
+    sh.seq_words = seq_words_for(max_len);
+    sh.gbytes = (uint32_t)group_smem_bytes<T>(max_len, cigar_stride);
+    return sh;
+}
+
+template <class T>
+int grid_of(uint32_t max_len, uint32_t cigar_stride, int sm_count)
+{
+    return shape_of<T>(max_len, cigar_stride, sm_count).grid;
 }
 
 template <class T>
@@ -341,7 +431,8 @@ history_cigar_kernel(Layout L, uint32_t n, uint32_t max_len, const int32_t* dist
     uint2* QP = reinterpret_cast<uint2*>(gs);
     uint2* QT = QP + seq_words;
     uint8_t* chain = gs + 16u * (size_t)seq_words;
-    int8_t* stage = reinterpret_cast<int8_t*>(chain + 64);
+    int* runs = reinterpret_cast<int*>(chain + 64);
+    int8_t* stage = reinterpret_cast<int8_t*>(chain + 64 + 256);
     const uint32_t step = gridDim.x * (uint32_t)(kWarps * GPW);
     for (uint32_t wb = (blockIdx.x * kWarps + (uint32_t)warp) * GPW; wb < n; wb += step) {
         const uint32_t pi = wb + (uint32_t)grp;
@@ -357,14 +448,14 @@ history_cigar_kernel(Layout L, uint32_t n, uint32_t max_len, const int32_t* dist
             }
             continue;
         }
-        load_packed<G>(pr.p, pr.plen, QP, g, gmask);
-        load_packed<G>(pr.t, pr.tlen, QT, g, gmask);
+        load_packed<G, 3>(pr.p, pr.plen, QP, g, gmask);
+        load_packed<G, 3>(pr.t, pr.tlen, QT, g, gmask);
         const uint64_t w0 = hist[2u * pi], w1 = hist[2u * pi + 1u];
         for (int d = g; d < D; d += G)
             chain[d] = (uint8_t)(((d < 32 ? w0 : w1) >> (2 * (d & 31))) & 3u);
         __syncwarp(gmask);
-        CigarSink sink{stage, stride, 0u};
-        int len = replay_chain<G>(QP, QT, (int)pr.plen, (int)pr.tlen, chain, D, sink, g, grp, gmask);
+        int len = replay_chain<G>(QP, QT, (int)pr.plen, (int)pr.tlen, chain, D, runs, stage, stride, g,
+                                  grp, gmask);
         const bool bad = len < 0;
         if (bad) len = -1 - len;
         if (stride) store_cigar<G>(stage, (uint32_t)len, stride, cigar + (size_t)pi * stride, g, gmask);
@@ -386,6 +477,18 @@ size_t tier_scratch_bytes(int tier, int grid)
     case 3: return T3::ops_bytes * (size_t)grid * (kWarps * T3::GPW);
     case 4: return T4::ops_bytes * (size_t)grid * (kWarps * T4::GPW);
     default: return 0;
+    }
+}
+
+TierShape tier_shape(int tier, uint32_t max_len, uint32_t cigar_stride, int sm_count)
+{
+    switch (tier) {
+    case 0: return shape_of<T0>(max_len, cigar_stride, sm_count);
+    case 1: return shape_of<T1>(max_len, cigar_stride, sm_count);
+    case 2: return shape_of<T2>(max_len, cigar_stride, sm_count);
+    case 3: return shape_of<T3>(max_len, cigar_stride, sm_count);
+    case 4: return shape_of<T4>(max_len, cigar_stride, sm_count);
+    default: return TierShape{};
     }
 }
 
@@ -429,7 +532,7 @@ cudaError_t launch_cigar_from_history(const Layout& L, uint32_t n, uint32_t max_
 {
     if (n == 0) return cudaSuccess;
     const uint32_t sw = seq_words_for(max_len);
-    const size_t gb = 16u * (size_t)sw + 64u + round16(stride);
+    const size_t gb = 16u * (size_t)sw + 64u + 256u + round16(stride);
     const size_t smem = gb * (size_t)(kWarps * (32 / kHG));
     if (smem > 227u * 1024u) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(history_cigar_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -21,6 +21,26 @@ struct TierInfo {
 constexpr int kNumTiers = 5;
 const TierInfo& tier_info(int t);
 
+/* Launch shape of one tier, for launches made on the device. */
+struct TierShape {
+    int grid;           /* persistent grid (resident CTAs) */
+    uint32_t smem;      /* dynamic shared memory per CTA */
+    uint32_t seq_words; /* 16-base words per sequence in shared memory */
+    uint32_t gbytes;    /* shared memory per group */
+};
+
+/* The tier chain of one batch.  Each tier kernel's last CTA launches the
+ * next tier as a tail launch when it handed any pair on, so no launch is
+ * made for a tier that has no work. */
+struct Chain {
+    int last_tier;                   /* last tier of the chain */
+    TierShape shape[kNumTiers];
+    uint32_t* lists[2];              /* work lists, used alternately by the tiers */
+    uint32_t* counts;                /* counts[t]: pairs tier t handed on */
+    uint32_t* cta_done;              /* cta_done[t]: CTAs of tier t that finished */
+    unsigned long long* launched;    /* launched[t]: launches of tier t (stats) */
+};
+
 /* Arguments of one alignment launch over a work list. */
 struct AlignLaunch {
     Layout L;
@@ -39,7 +59,13 @@ struct AlignLaunch {
     unsigned long long* passed_total; /* running count of pairs handed on (stats) */
     unsigned char* ops_scratch;  /* global op store for tiers that keep it there */
     size_t ops_scratch_bytes;
+    int tier;                    /* this launch's tier */
+    Chain chain;                 /* chain.cta_done == NULL: no device-side chaining */
 };
+
+/* Launch shape of tier t for sequences up to max_len and CIGAR slots of
+ * cigar_stride: persistent grid sized by occupancy (grid 0: does not fit). */
+TierShape tier_shape(int tier, uint32_t max_len, uint32_t cigar_stride, int sm_count);
 
 /* Bytes of global op-store scratch tier t needs for `grid` CTAs. */
 size_t tier_scratch_bytes(int tier, int grid);

@@ -98,6 +98,7 @@ extern "C" int wfe_align_device_noalloc(const char* d_ascii, const wfe_pair* d_p
     a.passed_total = nullptr;
     a.ops_scratch = static_cast<unsigned char*>(scratch);
     a.ops_scratch_bytes = kNoallocScratchBytes;
+    a.tier = kNoallocTier; /* a.chain.cta_done stays NULL: no tier follows */
     const cudaError_t e = wfe::launch_tier(kNoallocTier, a, grid, static_cast<cudaStream_t>(stream));
     return e == cudaSuccess ? WFE_OK : WFE_ERR_CUDA;
 }
