@@ -370,13 +370,39 @@ struct HostJob {
     const uint32_t* t_len;
 };
 
+/* Device address of a pinned, device-mapped host buffer (NULL when p is
+ * pageable or not host memory). */
+void* mapped_address(const void* p)
+{
+    if (!p) return nullptr;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError(); /* pageable memory of an older driver: not mapped */
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 int align_host(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, int8_t* cigar_out,
                uint8_t* status_out)
 {
     const wfe_config& c = ctx->cfg;
     WFE_CUDA(ctx, cudaSetDevice(c.device));
+    const bool want_cigar = cigar_out && c.cigar_stride;
+
+    /* pinned inputs are read in place, pinned outputs written in place */
+    const char* m_ascii = (const char*)mapped_address(job.ascii);
+    const wfe_pair* m_pairs = job.pairs ? (const wfe_pair*)mapped_address(job.pairs) : nullptr;
+    const uint32_t* m_plen = job.pairs ? nullptr : (const uint32_t*)mapped_address(job.p_len);
+    const uint32_t* m_tlen = job.pairs ? nullptr : (const uint32_t*)mapped_address(job.t_len);
+    const bool in_place = m_ascii && job.ascii_bytes > 0 && (job.pairs ? m_pairs != nullptr : (m_plen && m_tlen));
+    int32_t* m_dist = (int32_t*)mapped_address(dist_out);
+    int8_t* m_cigar = want_cigar ? (int8_t*)mapped_address(cigar_out) : nullptr;
+    uint8_t* m_status = status_out ? (uint8_t*)mapped_address(status_out) : nullptr;
+    const bool out_in_place = m_dist && (!want_cigar || m_cigar) && (!status_out || m_status);
+
     size_t B = c.batch_size;
-    if (!job.pairs) {
+    if (!job.pairs && !in_place) {
         /* strided slots may be wider than max_seq_len: fewer pairs per batch */
         const size_t fit = (ctx->st[0].ascii_cap - 32u) / (2u * job.stride);
         if (fit == 0) return WFE_ERR_SEQ_TOO_LONG;
@@ -390,16 +416,31 @@ int align_host(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, in
         cudaStream_t s = st.stream;
         nb = std::min(B, n - b0);
         Layout L{};
-        if (job.pairs) {
+        if (in_place) {
+            /* the kernels read the pinned inputs over the CPU-GPU link and
+             * check every pair against the buffer */
+            L.ascii = m_ascii;
+            L.ascii_bytes = job.ascii_bytes;
+            if (job.pairs) {
+                L.pairs = m_pairs + b0;
+            } else {
+                L.ascii = m_ascii + 2u * b0 * job.stride;
+                L.ascii_bytes = 2u * nb * job.stride;
+                L.plen = m_plen + b0;
+                L.tlen = m_tlen + b0;
+                L.stride = job.stride;
+            }
+            ctx->stats.mapped_batches++;
+        } else if (job.pairs) {
             const wfe_pair* P = job.pairs + b0;
-            uint64_t lo = UINT64_MAX, hi = 0, bases = 0;
+            uint64_t lo = UINT64_MAX, hi = 0;
             for (size_t i = 0; i < nb; ++i) {
                 if (P[i].p_len > c.max_seq_len || P[i].t_len > c.max_seq_len) return WFE_ERR_SEQ_TOO_LONG;
                 const uint64_t pe = P[i].p_off + P[i].p_len, te = P[i].t_off + P[i].t_len;
-                if (pe > job.ascii_bytes || te > job.ascii_bytes) return WFE_ERR_INVALID_ARGUMENT;
+                if (pe > job.ascii_bytes || te > job.ascii_bytes || pe < P[i].p_off || te < P[i].t_off)
+                    return WFE_ERR_INVALID_ARGUMENT;
                 lo = std::min(lo, std::min(P[i].p_off, P[i].t_off));
                 hi = std::max(hi, std::max(pe, te));
-                bases += (uint64_t)P[i].p_len + P[i].t_len;
             }
             if (nb == 0 || hi <= lo) lo = hi = 0;
             if (hi - lo + 32u <= st.ascii_cap) {
@@ -413,7 +454,7 @@ int align_host(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, in
                 WFE_CUDA(ctx, cudaStreamSynchronize(s));
                 if (!st.h_stage) {
                     WFE_CUDA(ctx, cudaMallocHost(&st.h_stage, st.ascii_cap));
-                    WFE_CUDA(ctx, cudaMallocHost(&st.h_pairs, B * sizeof(wfe_pair)));
+                    WFE_CUDA(ctx, cudaMallocHost(&st.h_pairs, c.batch_size * sizeof(wfe_pair)));
                 }
                 uint64_t pos = 0;
                 for (size_t i = 0; i < nb; ++i) {
@@ -430,7 +471,6 @@ int align_host(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, in
                 WFE_CUDA(ctx, cudaMemcpyAsync(st.d_pairs, st.h_pairs, nb * sizeof(wfe_pair), cudaMemcpyHostToDevice, s));
                 ctx->stats.h2d_bytes += pos + nb * sizeof(wfe_pair);
                 L.base_off = 0;
-                (void)bases;
             }
             L.ascii = st.d_ascii;
             L.pairs = st.d_pairs;
@@ -452,18 +492,25 @@ int align_host(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, in
             L.tlen = st.d_tlen;
             L.stride = job.stride;
         }
-        const int r = run_chain(ctx, st, L, (uint32_t)nb, st.d_dist, st.d_cigar, st.d_status, s);
-        if (r != WFE_OK) return r;
-        WFE_CUDA(ctx, cudaMemcpyAsync(dist_out + b0, st.d_dist, nb * 4u, cudaMemcpyDeviceToHost, s));
-        ctx->stats.d2h_bytes += nb * 4u;
-        if (status_out) {
-            WFE_CUDA(ctx, cudaMemcpyAsync(status_out + b0, st.d_status, nb, cudaMemcpyDeviceToHost, s));
-            ctx->stats.d2h_bytes += nb;
-        }
-        if (cigar_out && c.cigar_stride) {
-            WFE_CUDA(ctx, cudaMemcpyAsync(cigar_out + b0 * c.cigar_stride, st.d_cigar, nb * c.cigar_stride,
-                                          cudaMemcpyDeviceToHost, s));
-            ctx->stats.d2h_bytes += nb * c.cigar_stride;
+        if (out_in_place) {
+            const int r = run_chain(ctx, st, L, (uint32_t)nb, m_dist + b0,
+                                    want_cigar ? m_cigar + b0 * c.cigar_stride : nullptr,
+                                    status_out ? m_status + b0 : nullptr, s);
+            if (r != WFE_OK) return r;
+        } else {
+            const int r = run_chain(ctx, st, L, (uint32_t)nb, st.d_dist, st.d_cigar, st.d_status, s);
+            if (r != WFE_OK) return r;
+            WFE_CUDA(ctx, cudaMemcpyAsync(dist_out + b0, st.d_dist, nb * 4u, cudaMemcpyDeviceToHost, s));
+            ctx->stats.d2h_bytes += nb * 4u;
+            if (status_out) {
+                WFE_CUDA(ctx, cudaMemcpyAsync(status_out + b0, st.d_status, nb, cudaMemcpyDeviceToHost, s));
+                ctx->stats.d2h_bytes += nb;
+            }
+            if (want_cigar) {
+                WFE_CUDA(ctx, cudaMemcpyAsync(cigar_out + b0 * c.cigar_stride, st.d_cigar,
+                                              nb * c.cigar_stride, cudaMemcpyDeviceToHost, s));
+                ctx->stats.d2h_bytes += nb * c.cigar_stride;
+            }
         }
         ctx->stats.batches++;
         ctx->stats.pairs += nb;
@@ -518,6 +565,56 @@ int wfe_cigar_from_history_device(const char* d_ascii, const wfe_pair* d_pairs, 
     const cudaError_t e = launch_cigar_from_history(L, (uint32_t)n, max_len, d_dist, d_history, d_cigar,
                                                     cigar_stride, d_status, (cudaStream_t)stream);
     return e == cudaSuccess ? WFE_OK : WFE_ERR_CUDA;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int wfe_device_count(int* count)
+{
+    if (!count) return WFE_ERR_INVALID_ARGUMENT;
+    *count = 0;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return WFE_ERR_NO_DEVICE;
+    }
+    *count = n;
+    return n > 0 ? WFE_OK : WFE_ERR_NO_DEVICE;
+}
+
+int wfe_device_name(int device, char* name, size_t cap, int* cc_major, int* cc_minor)
+{
+    cudaDeviceProp prop{};
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) {
+        cudaGetLastError();
+        return WFE_ERR_NO_DEVICE;
+    }
+    if (name && cap) {
+        std::strncpy(name, prop.name, cap - 1);
+        name[cap - 1] = 0;
+    }
+    if (cc_major) *cc_major = prop.major;
+    if (cc_minor) *cc_minor = prop.minor;
+    return WFE_OK;
+}
+
+int wfe_host_alloc(void** p, size_t bytes)
+{
+    if (!p) return WFE_ERR_INVALID_ARGUMENT;
+    *p = nullptr;
+    const cudaError_t e = cudaMallocHost(p, bytes ? bytes : 1);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return e == cudaErrorMemoryAllocation ? WFE_ERR_OUT_OF_MEMORY : WFE_ERR_CUDA;
+    }
+    return WFE_OK;
+}
+
+void wfe_host_free(void* p)
+{
+    if (p) cudaFreeHost(p);
 }
 
 }  // extern "C"

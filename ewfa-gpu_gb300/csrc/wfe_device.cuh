@@ -48,28 +48,35 @@ struct Layout {
     const uint32_t* tlen;
     uint64_t stride;        /* strided layout: pattern i at 2*i*stride, text at (2i+1)*stride */
     uint64_t base_off;      /* descriptor offsets are relative to ascii - base_off */
+    uint64_t ascii_bytes;   /* descriptor bytes must lie below this offset (0 = unchecked) */
 };
 
 struct PairRef {
     const char* p;
     const char* t;
     uint32_t plen, tlen;
+    bool in_range;          /* both sequences lie inside the checked buffer */
 };
 
 __device__ __forceinline__ PairRef get_pair(const Layout& L, uint32_t i)
 {
     PairRef r;
+    r.in_range = true;
     if (L.pairs) {
         const wfe_pair d = L.pairs[i];
         r.p = L.ascii + (d.p_off - L.base_off);
         r.t = L.ascii + (d.t_off - L.base_off);
         r.plen = d.p_len;
         r.tlen = d.t_len;
+        if (L.ascii_bytes)
+            r.in_range = d.p_off <= L.ascii_bytes && d.p_len <= L.ascii_bytes - d.p_off &&
+                         d.t_off <= L.ascii_bytes && d.t_len <= L.ascii_bytes - d.t_off;
     } else {
         r.p = L.ascii + 2ull * i * L.stride;
         r.t = r.p + L.stride;
         r.plen = L.plen[i];
         r.tlen = L.tlen[i];
+        if (L.ascii_bytes) r.in_range = r.plen <= L.stride && r.tlen <= L.stride;
     }
     return r;
 }

@@ -33,7 +33,7 @@ namespace {
 constexpr int kWarps = 4;
 constexpr int kThreads = kWarps * 32;
 
-enum : int { ST_IDLE = 0, ST_RUN, ST_DONE, ST_OVERFLOW, ST_OVERMAX, ST_TOOLONG, ST_BADWALK };
+enum : int { ST_IDLE = 0, ST_RUN, ST_DONE, ST_OVERFLOW, ST_OVERMAX, ST_TOOLONG, ST_BADWALK, ST_RANGE };
 
 __host__ __device__ constexpr size_t round16(size_t x) { return (x + 15u) & ~size_t(15); }
 
@@ -203,7 +203,8 @@ tier_kernel(AlignLaunch A, uint32_t seq_words, uint32_t gbytes)
             pi = A.work ? A.work[item] : item;
             pr = get_pair(A.L, pi);
             const uint32_t mx = max(pr.plen, pr.tlen);
-            state = (mx > A.max_len || mx > 16u * seq_words) ? ST_TOOLONG : ST_RUN;
+            state = !pr.in_range ? ST_RANGE
+                    : (mx > A.max_len || mx > 16u * seq_words) ? ST_TOOLONG : ST_RUN;
         }
         const uint32_t lp = state == ST_RUN ? pr.plen : 0u;
         const uint32_t lt = state == ST_RUN ? pr.tlen : 0u;
@@ -314,12 +315,13 @@ tier_kernel(AlignLaunch A, uint32_t seq_words, uint32_t gbytes)
                 if (A.passed_total) atomicAdd(A.passed_total, 1ull);
             }
         } else if (state == ST_OVERFLOW || state == ST_OVERMAX || state == ST_TOOLONG ||
-                   state == ST_BADWALK) {
+                   state == ST_BADWALK || state == ST_RANGE) {
             if (g == 0) {
                 A.dist[pi] = state == ST_OVERMAX ? A.max_distance + 1 : -1;
                 if (A.status)
                     A.status[pi] = state == ST_OVERMAX  ? (uint8_t)WFE_PAIR_OVER_MAX_DISTANCE
                                    : state == ST_BADWALK ? (uint8_t)WFE_PAIR_BAD_HISTORY
+                                   : state == ST_RANGE   ? (uint8_t)WFE_PAIR_OUT_OF_RANGE
                                                          : (uint8_t)WFE_PAIR_TOO_LONG;
                 if (A.cigar_stride) A.cigar[(size_t)pi * A.cigar_stride] = 0;
             }

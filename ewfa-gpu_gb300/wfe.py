@@ -22,6 +22,7 @@ OK = 0
 ERR_INVALID_ARGUMENT, ERR_OUT_OF_MEMORY, ERR_SEQ_TOO_LONG, ERR_CUDA = 1, 2, 3, 4
 ERR_NO_DEVICE, ERR_TIMEOUT, ERR_BUSY, ERR_INTERNAL, ERR_NOT_FOUND = 5, 6, 7, 8, 9
 PAIR_OK, PAIR_OVER_MAX_DISTANCE, PAIR_CIGAR_TRUNCATED, PAIR_TOO_LONG, PAIR_BAD_HISTORY = 0, 1, 2, 3, 4
+PAIR_OUT_OF_RANGE = 5
 FLAG_NO_PIPELINE = 1
 FLAG_KERNEL_TIMING = 2
 
@@ -52,7 +53,7 @@ class Stats(C.Structure):
     _fields_ = [("pairs", C.c_uint64), ("batches", C.c_uint64), ("kernel_launches", C.c_uint64),
                 ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("tier_entered", C.c_uint64 * 8),
                 ("tier_passed", C.c_uint64 * 8), ("tier_launches", C.c_uint64 * 8),
-                ("tier_ms", C.c_double * 8)]
+                ("tier_ms", C.c_double * 8), ("mapped_batches", C.c_uint64)]
 
 
 class GenConfig(C.Structure):
@@ -239,7 +240,8 @@ class Context:
         return {"pairs": s.pairs, "batches": s.batches, "kernel_launches": s.kernel_launches,
                 "h2d_bytes": s.h2d_bytes, "d2h_bytes": s.d2h_bytes,
                 "tier_entered": list(s.tier_entered), "tier_passed": list(s.tier_passed),
-                "tier_launches": list(s.tier_launches), "tier_ms": list(s.tier_ms)}
+                "tier_launches": list(s.tier_launches), "tier_ms": list(s.tier_ms),
+                "mapped_batches": s.mapped_batches}
 
     def reset_stats(self) -> None:
         _check(load().wfe_reset_stats(self._h), "wfe_reset_stats")

@@ -57,10 +57,13 @@ enum {
                                        terminator (the reference overflows into
                                        the next slot instead) */
     WFE_PAIR_TOO_LONG = 3,          /* sequence longer than the launch's capacity */
-    WFE_PAIR_BAD_HISTORY = 4        /* history holds a code that is not an
+    WFE_PAIR_BAD_HISTORY = 4,       /* history holds a code that is not an
                                        operation: the CIGAR stops there (the
                                        reference's "Incorrect backtrace" exit,
                                        src/kernels.cu:471-478) */
+    WFE_PAIR_OUT_OF_RANGE = 5       /* the pair's bytes lie outside the ASCII
+                                       buffer (host calls that read it in place);
+                                       the pair is not aligned */
 };
 
 /* One pattern/text pair inside a caller buffer of ASCII bases.  Any byte is a
@@ -104,8 +107,10 @@ typedef struct wfe_stats {
     uint64_t tier_passed[8];   /* pairs each tier handed on to the next (above
                                   its distance capacity) */
     uint64_t tier_launches[8]; /* launches of each tier's kernel */
-    double tier_ms[8];         /* GPU milliseconds of those launches (only with
-                                  WFE_FLAG_KERNEL_TIMING) */
+    double tier_ms[8];         /* GPU milliseconds of the chains started at each
+                                  tier (only with WFE_FLAG_KERNEL_TIMING) */
+    uint64_t mapped_batches;   /* host-call batches whose pinned inputs the
+                                  kernels read in place */
 } wfe_stats;
 
 /* ---- lifecycle -------------------------------------------------------- */
@@ -134,11 +139,21 @@ int wfe_reset_stats(wfe_ctx* ctx);
 
 /* Align n pairs held in HOST memory; results to HOST memory.  Replaces the
  * loop GPU_launch_wavefront_distance / prepare_next_batch
- * (src/aligner.cu:63-65, src/wavefront.cu:173-330): batches of batch_size
- * pairs are copied in, packed, aligned, their CIGARs generated and copied
- * back, with the copies of one batch overlapping the kernels of another.
- * dist_out[n], cigar_out[n * cigar_stride], status_out[n] (may be NULL).
- * Synchronous: returns when every result is in host memory. */
+ * (src/aligner.cu:63-65, src/wavefront.cu:173-330), in batches of
+ * batch_size pairs.  dist_out[n], cigar_out[n * cigar_stride], status_out[n]
+ * (may be NULL).  Synchronous: returns when every result is in host memory.
+ *
+ * Pinned (page-locked, device-mapped) buffers are used in place: when the
+ * ASCII buffer and the descriptors are pinned, the kernels read them directly
+ * over the CPU-GPU link (NVLink-C2C on GB300) with no staging copy, checking
+ * every descriptor against ascii_bytes (pairs outside get
+ * WFE_PAIR_OUT_OF_RANGE) and every length against max_seq_len
+ * (WFE_PAIR_TOO_LONG); when the outputs are pinned, the kernels write them
+ * directly.  Pageable buffers are staged: each batch's span of ASCII and its
+ * descriptors are copied in (the call then returns WFE_ERR_SEQ_TOO_LONG or
+ * WFE_ERR_INVALID_ARGUMENT for bad pairs before aligning anything), results
+ * copied out, with the copies of one batch overlapping the kernels of the
+ * other. */
 int wfe_align(wfe_ctx* ctx, const char* ascii, size_t ascii_bytes,
               const wfe_pair* pairs, size_t n, int32_t* dist_out,
               int8_t* cigar_out, uint8_t* status_out);
@@ -225,6 +240,22 @@ int wfe_align_device_noalloc(const char* d_ascii, const wfe_pair* d_pairs, size_
                              uint32_t max_len, int32_t max_distance, int32_t* d_dist,
                              int8_t* d_cigar, uint32_t cigar_stride, uint8_t* d_status,
                              void* stream);
+
+/* ---- host helpers --------------------------------------------------------- */
+
+/* Number of CUDA devices (0 when there is none or no driver).  Replaces
+ * cudaGetDeviceCount in src/aligner.cu:140-145. */
+int wfe_device_count(int* count);
+
+/* Name and compute capability of a device, for the CLI's banner
+ * (src/aligner.cu:147-151). */
+int wfe_device_name(int device, char* name, size_t cap, int* cc_major, int* cc_minor);
+
+/* Page-locked, device-mapped host memory: buffers in it are read and written
+ * by the kernels in place (see wfe_align).  Replaces the reader's
+ * cudaMallocHost (utils/sequence_reader.cu:77-86). */
+int wfe_host_alloc(void** p, size_t bytes);
+void wfe_host_free(void* p);
 
 /* ---- host CIGAR utilities ---------------------------------------------- */
 

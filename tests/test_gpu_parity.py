@@ -282,3 +282,80 @@ def test_full_short_read_workload_properties():
     od, ocg, ost, _ = oracle_run(sub_ascii, sub_pairs, 152)
     np.testing.assert_array_equal(dist[sample], od)
     assert_same_cigars(cg[sample], ocg)
+
+
+def _pinned(a):
+    import torch
+    t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(a.dtype).reshape(a.shape)
+    t[...] = a
+    return t
+
+
+def test_pinned_buffers_read_and_written_in_place():
+    """Pinned inputs are read by the kernels in place (no staging copy) and
+    pinned outputs written in place; results equal the staged path's, for
+    every combination, with both input layouts."""
+    torch_cuda()
+    ascii, pairs = wfe.generate(30000, 150, p_min=0.05, seed=13)
+    stride = 152
+    with wfe.Context(max_seq_len=300, batch_size=7000, cigar_stride=stride) as ctx:
+        want = ctx.align(ascii, pairs)
+        assert ctx.stats()["mapped_batches"] == 0
+        for pin_in in (False, True):
+            for pin_out in (False, True):
+                a = _pinned(ascii) if pin_in else ascii
+                p = _pinned(pairs) if pin_in else pairs
+                n = len(pairs)
+                out = (np.zeros(n, np.int32), np.zeros((n, stride), np.int8), np.zeros(n, np.uint8))
+                if pin_out:
+                    out = tuple(_pinned(o) for o in out)
+                ctx.reset_stats()
+                got = ctx.align(a, p, out=out)
+                assert (ctx.stats()["mapped_batches"] > 0) == pin_in
+                np.testing.assert_array_equal(got[0], want[0])
+                np.testing.assert_array_equal(got[2], want[2])
+                assert_same_cigars(got[1], want[1])
+    compare_with_oracle(ascii, pairs, stride, *want)
+
+
+def test_pinned_bad_descriptors_flagged_per_pair():
+    """In place, a descriptor outside the buffer or a sequence over
+    max_seq_len is reported per pair; nothing outside the buffer is read."""
+    torch_cuda()
+    ascii, pairs = wfe.generate(200, 150, p_min=0.05, seed=14)
+    pairs = pairs.copy()
+    pairs[3]["p_off"] = len(ascii) + 1000          # beyond the buffer
+    pairs[5]["t_len"] = len(ascii)                 # runs past the end
+    pairs[7]["p_off"] = np.uint64(2**63)           # wraps
+    a, p = _pinned(ascii), _pinned(pairs)
+    with wfe.Context(max_seq_len=160, cigar_stride=152) as ctx:
+        d, cg, st = ctx.align(a, p)
+    assert st[3] == wfe.PAIR_OUT_OF_RANGE and st[5] == wfe.PAIR_OUT_OF_RANGE and st[7] == wfe.PAIR_OUT_OF_RANGE
+    too_long = (pairs["p_len"] > 160) | (pairs["t_len"] > 160)
+    too_long[[3, 5, 7]] = False
+    assert (st[too_long] == wfe.PAIR_TOO_LONG).all()
+    ok = np.ones(len(pairs), bool)
+    ok[[3, 5, 7]] = False
+    ok &= ~too_long
+    assert (st[ok] == wfe.PAIR_OK).all()
+    od, ocg, ost, _ = oracle_run(ascii, pairs[ok], 152)
+    np.testing.assert_array_equal(d[ok], od)
+
+
+def test_pinned_strided_layout():
+    torch_cuda()
+    seqs = []
+    ascii, pairs = wfe.generate(3000, 140, p_min=0.05, seed=15)
+    unp = 304
+    buf = np.zeros(2 * unp * len(pairs), np.uint8)
+    for i, q in enumerate(pairs):
+        buf[2 * i * unp: 2 * i * unp + q["p_len"]] = ascii[q["p_off"]: q["p_off"] + q["p_len"]]
+        buf[(2 * i + 1) * unp: (2 * i + 1) * unp + q["t_len"]] = ascii[q["t_off"]: q["t_off"] + q["t_len"]]
+    pl, tl = pairs["p_len"].copy(), pairs["t_len"].copy()
+    with wfe.Context(max_seq_len=300, batch_size=1000) as ctx:
+        want = ctx.align_strided(buf, unp, pl, tl)
+        got = ctx.align_strided(_pinned(buf), unp, _pinned(pl), _pinned(tl))
+        assert ctx.stats()["mapped_batches"] == 3
+    np.testing.assert_array_equal(got[0], want[0])
+    assert_same_cigars(got[1], want[1])
+    compare_with_oracle(ascii, pairs, 152, *want)
