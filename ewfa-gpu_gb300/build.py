@@ -31,7 +31,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wextra", f"-I{INC}", f"-I{
 CC_FLAGS = ["-O2", "-std=c11", "-fPIC", "-Wall", "-Wextra", "-ffp-contract=off", f"-I{INC}", f"-I{CSRC}"]
 
 LIB_CU = ["wfe_kernels.cu", "wfe_api.cu", "wfe_noalloc.cu"]
-LIB_CXX = ["wfe_host.cpp"]
+LIB_CXX = ["wfe_host.cpp", "seqfile.cpp"]
 
 
 def _nvcc() -> str:
@@ -99,7 +99,7 @@ def build(verbose: bool = False) -> dict:
     # command-line tools, linked against the shared library
     cuda_lib = os.path.join(_cuda_home(), "lib64")
     tools = {
-        "wfe.aligner": (["aligner.cpp", "seqfile.cpp"], ["-lwfe"]),
+        "wfe.aligner": (["aligner.cpp"], ["-lwfe"]),
         "wfe.gen": (["gen_main.c"], ["-lwfe_gen"]),
     }
     for name, (srcs, libs) in tools.items():

@@ -32,7 +32,6 @@
 #include <thread>
 #include <vector>
 
-#include "seqfile.h"
 #include "wfe.h"
 
 namespace {
@@ -168,12 +167,18 @@ int main(int argc, char** argv)
     }
 
     /* read the file before the clock starts, like the reference */
-    wfe::PairFile pf;
-    if (!wfe::read_pair_file(path, (size_t)n_req, (int)std::thread::hardware_concurrency(), true, pf)) {
-        std::fprintf(stderr, "%s\n", pf.error.c_str());
+    wfe_pair_file pf{};
+    char err[256] = {0};
+    if (wfe_read_pair_file(path.c_str(), (size_t)n_req, (int)std::thread::hardware_concurrency(), 1, &pf, err,
+                           sizeof err) != WFE_OK) {
+        std::fprintf(stderr, "%s\n", err);
         std::fprintf(stderr, "Could not read the sequences from file %s\n", path.c_str());
         return 1;
     }
+    struct Release {
+        wfe_pair_file* f;
+        ~Release() { wfe_free_pair_file(f); }
+    } release{&pf};
     const uint32_t max_len = (uint32_t)(2 * seq_len); /* the reader's slot holds 2*l bases */
     if (pf.longest > max_len) {
         std::fprintf(stderr, "A sequence of %u bases is longer than 2*l = %u.\n", pf.longest, max_len);
@@ -221,12 +226,12 @@ int main(int argc, char** argv)
         /* the pairs of this share: in the file's pinned descriptors, or the
          * empty tail */
         if (sh.first + sh.n <= pf.n) {
-            sh.rc = wfe_align(ctx, pf.data, pf.bytes, pf.pairs + sh.first, sh.n, sh.dist.data(), sh.cigar.data(),
+            sh.rc = wfe_align(ctx, pf.ascii, pf.ascii_bytes, pf.pairs + sh.first, sh.n, sh.dist.data(), sh.cigar.data(),
                               sh.status.data());
         } else {
             std::vector<wfe_pair> mine(sh.n);
             for (size_t i = 0; i < sh.n; ++i) mine[i] = *pair_at(sh.first + i);
-            sh.rc = wfe_align(ctx, pf.data, pf.bytes, mine.data(), sh.n, sh.dist.data(), sh.cigar.data(),
+            sh.rc = wfe_align(ctx, pf.ascii, pf.ascii_bytes, mine.data(), sh.n, sh.dist.data(), sh.cigar.data(),
                               sh.status.data());
         }
         if (sh.rc != WFE_OK) sh.what = "wfe_align";
@@ -264,7 +269,7 @@ int main(int argc, char** argv)
                 }
                 const wfe_pair* q = pair_at(sh.first + i);
                 int32_t score = -1;
-                if (wfe_check_cigar(pf.data + q->p_off, q->p_len, pf.data + q->t_off, q->t_len,
+                if (wfe_check_cigar(pf.ascii + q->p_off, q->p_len, pf.ascii + q->t_off, q->t_len,
                                     &sh.cigar[i * stride], stride, &score) && score == sh.dist[i])
                     ++good;
             }

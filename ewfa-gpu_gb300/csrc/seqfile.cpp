@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <new>
 #include <thread>
 
 namespace wfe {
@@ -161,9 +162,10 @@ bool read_pair_file(const std::string& path, size_t max_pairs, int nthreads, boo
                 q.t_off = off;
                 q.t_len = (uint32_t)len;
             } else {
+                /* the text fields belong to the text line, which another
+                 * thread may be writing; a missing text line leaves them 0 */
                 q.p_off = off;
                 q.p_len = (uint32_t)len;
-                q.t_off = off; /* a missing text line leaves an empty text */
             }
             longest[t] = std::max(longest[t], (uint32_t)len);
             ++li;
@@ -187,3 +189,44 @@ bool read_pair_file(const std::string& path, size_t max_pairs, int nthreads, boo
 }
 
 }  // namespace wfe
+
+extern "C" int wfe_read_pair_file(const char* path, size_t max_pairs, int nthreads, int pin, wfe_pair_file* out,
+                                  char* err, size_t err_cap)
+{
+    if (!path || !out) return WFE_ERR_INVALID_ARGUMENT;
+    std::memset(out, 0, sizeof *out);
+    wfe::PairFile* pf = new (std::nothrow) wfe::PairFile();
+    if (!pf) return WFE_ERR_OUT_OF_MEMORY;
+    if (!wfe::read_pair_file(path, max_pairs, nthreads, pin != 0, *pf)) {
+        if (err && err_cap) {
+            std::strncpy(err, pf->error.c_str(), err_cap - 1);
+            err[err_cap - 1] = 0;
+        }
+        const bool oom = pf->error.find("allocate") != std::string::npos;
+        delete pf;
+        return oom ? WFE_ERR_OUT_OF_MEMORY : WFE_ERR_INVALID_ARGUMENT;
+    }
+    out->ascii = pf->data;
+    out->ascii_bytes = pf->bytes;
+    out->pairs = pf->pairs;
+    out->n = pf->n;
+    out->longest = pf->longest;
+    out->pinned = pf->pinned ? 1 : 0;
+    pf->data = nullptr; /* ownership moves to *out */
+    pf->pairs = nullptr;
+    delete pf;
+    return WFE_OK;
+}
+
+extern "C" void wfe_free_pair_file(wfe_pair_file* f)
+{
+    if (!f) return;
+    if (f->pinned) {
+        wfe_host_free(f->ascii);
+        wfe_host_free(f->pairs);
+    } else {
+        std::free(f->ascii);
+        std::free(f->pairs);
+    }
+    std::memset(f, 0, sizeof *f);
+}

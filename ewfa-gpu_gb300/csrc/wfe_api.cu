@@ -55,6 +55,7 @@ struct wfe_ctx {
     wfe_config cfg{};
     int sm_count = 0;
     int first_tier = 0;
+    int last_tier = 0;      /* 5, or 6 when sequences can be longer than kLongSmemDistance */
     int grid[kNumTiers] = {};
     TierShape shape[kNumTiers] = {};
     unsigned char* d_ops_scratch = nullptr;
@@ -136,18 +137,18 @@ int run_chain(wfe_ctx* ctx, Stage& st, const Layout& L, uint32_t n, int32_t* dis
     a.status = status;
     a.max_distance = c.max_distance;
     a.max_len = c.max_seq_len;
-    a.retry = (t + 1 < kNumTiers) ? st.d_lists : nullptr;
     a.retry_count = st.d_counts + t;
     a.passed_total = ctx->d_passed + t;
     a.ops_scratch = ctx->d_ops_scratch;
     a.ops_scratch_bytes = ctx->ops_scratch_bytes;
     a.tier = t;
     /* a distance cap at or below a tier's capacity ends the chain there */
-    int last = kNumTiers - 1;
+    int last = ctx->last_tier;
     if (c.max_distance > 0)
         for (int u = t; u < kNumTiers; ++u)
             if (c.max_distance <= tier_info(u).dcap) { last = u; break; }
     a.chain.last_tier = last;
+    a.retry = t < last ? st.d_lists : nullptr;
     for (int u = 0; u < kNumTiers; ++u) a.chain.shape[u] = ctx->shape[u];
     a.chain.lists[0] = st.d_lists;
     a.chain.lists[1] = st.d_lists + B;
@@ -155,7 +156,7 @@ int run_chain(wfe_ctx* ctx, Stage& st, const Layout& L, uint32_t n, int32_t* dis
     a.chain.cta_done = st.d_counts + kNumTiers;
     a.chain.launched = ctx->d_launched;
     const TierInfo& ti = tier_info(t);
-    const uint32_t per_cta = 4u * (32u / (uint32_t)ti.G);
+    const uint32_t per_cta = t >= 5 ? 1u : 4u * (32u / (uint32_t)ti.G);
     int grid = (int)std::min<uint64_t>((uint64_t)ctx->grid[t], ((uint64_t)n + per_cta - 1) / per_cta);
     grid = std::max(grid, 1);
     TimedLaunch tl{t, nullptr, nullptr};
@@ -233,6 +234,7 @@ int wfe_create(const wfe_config* cfg, wfe_ctx** out)
         for (auto& s : ctx->st) free_stage(s);
         cudaFree(ctx->d_ops_scratch);
         cudaFree(ctx->d_passed);
+        for (auto& sh : ctx->shape) cudaFree(sh.scratch);
         delete ctx;
         return err == cudaErrorMemoryAllocation ? WFE_ERR_OUT_OF_MEMORY : WFE_ERR_CUDA;
     };
@@ -240,14 +242,25 @@ int wfe_create(const wfe_config* cfg, wfe_ctx** out)
     e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, c.device);
     if (e != cudaSuccess) return bail(e);
     size_t scratch = 0;
+    ctx->last_tier = c.max_seq_len > (uint32_t)kLongSmemDistance ? 6 : 5;
     for (int t = 0; t < kNumTiers; ++t) {
         ctx->shape[t] = tier_shape(t, c.max_seq_len, c.cigar_stride, ctx->sm_count);
         ctx->grid[t] = ctx->shape[t].grid;
         if (ctx->grid[t] <= 0) { /* sequences too long for this tier's shared memory */
-            if (t >= ctx->first_tier) return bail(cudaErrorInvalidValue);
+            if (t >= ctx->first_tier && t <= ctx->last_tier) return bail(cudaErrorInvalidValue);
             continue;
         }
-        scratch = std::max(scratch, tier_scratch_bytes(t, ctx->grid[t]));
+        if (t < 5) scratch = std::max(scratch, tier_scratch_bytes(t, ctx->grid[t]));
+    }
+    /* tiers 5-6: a scratch slab per resident CTA (backtrace store, chain,
+     * runs; tier 6 also its wavefront), the grid trimmed to a budget */
+    for (int t = 5; t <= ctx->last_tier; ++t) {
+        TierShape& sh = ctx->shape[t];
+        const uint64_t budget = t == 5 ? (2ull << 30) : (8ull << 30);
+        const uint64_t fit = std::max<uint64_t>(1, budget / sh.slab);
+        sh.grid = (int)std::min<uint64_t>((uint64_t)sh.grid, fit);
+        ctx->grid[t] = sh.grid;
+        if ((e = cudaMalloc(&sh.scratch, (size_t)sh.slab * sh.grid)) != cudaSuccess) return bail(e);
     }
     if (scratch) {
         e = cudaMalloc(&ctx->d_ops_scratch, scratch);
@@ -285,6 +298,7 @@ void wfe_destroy(wfe_ctx* ctx)
     }
     cudaFree(ctx->d_ops_scratch);
     cudaFree(ctx->d_passed);
+    for (auto& sh : ctx->shape) cudaFree(sh.scratch);
     for (auto& t : ctx->timed) {
         cudaEventDestroy(t.start);
         cudaEventDestroy(t.stop);

@@ -125,6 +125,9 @@ tier_kernel(AlignLaunch A, uint32_t seq_words, uint32_t gbytes);
 #define WFE_T0_MINB 8
 #endif
 using T0 = Tier<4, WFE_T0_J, true, 5, WFE_T0_MINB>; /* distance <= 4*J + 1 (21) */
+
+template <bool GLOBAL_WF>
+__global__ void __launch_bounds__(kLongThreads) long_kernel(AlignLaunch A);
 using T1 = Tier<32, 2, true, 1>;   /* distance <= 79  */
 using T2 = Tier<32, 4, true, 1>;   /* distance <= 143 */
 using T3 = Tier<32, 8, false, 1>;  /* distance <= 271 */
@@ -148,8 +151,8 @@ __device__ __noinline__ void launch_next_tier(const AlignLaunch& A, uint32_t cou
     n.tier = A.tier + 1;
     n.work = A.retry;
     n.work_count = A.retry_count;
-    n.retry = n.tier + 1 < kNumTiers ? (A.retry == A.chain.lists[0] ? A.chain.lists[1] : A.chain.lists[0])
-                                     : nullptr;
+    n.retry = n.tier < A.chain.last_tier ? (A.retry == A.chain.lists[0] ? A.chain.lists[1] : A.chain.lists[0])
+                                         : nullptr;
     n.retry_count = A.chain.counts + n.tier;
     n.passed_total = A.passed_total ? A.passed_total + 1 : nullptr;
     switch (n.tier) {
@@ -157,6 +160,17 @@ __device__ __noinline__ void launch_next_tier(const AlignLaunch& A, uint32_t cou
     case 2: launch_on_device<T2>(n, count); break;
     case 3: launch_on_device<T3>(n, count); break;
     case 4: launch_on_device<T4>(n, count); break;
+    case 5:
+    case 6: {
+        const TierShape& sh = n.chain.shape[n.tier];
+        const int grid = max(1, min(sh.grid, (int)count));
+        if (n.tier == 5)
+            long_kernel<false><<<grid, kLongThreads, sh.smem, cudaStreamTailLaunch>>>(n);
+        else
+            long_kernel<true><<<grid, kLongThreads, sh.smem, cudaStreamTailLaunch>>>(n);
+        if (n.chain.launched) atomicAdd(n.chain.launched + n.tier, 1ull);
+        break;
+    }
     default: break;
     }
 }
@@ -344,12 +358,193 @@ tier_kernel(AlignLaunch A, uint32_t seq_words, uint32_t gbytes)
     }
 }
 
+/* ------------------------------------------------------------------------ */
+/* Tiers 5 and 6: one CTA of 256 threads per pair, for distances beyond the
+ * register tiers.  Step d computes the 2d+1 cells of [-d, d] in 32-cell
+ * chunks, one warp per chunk (src/kernels.cu:111-180 with every thread of
+ * the CTA); a barrier separates the steps and every thread then tests the
+ * target cell (src/kernels.cu:268).  The wavefront's two buffers live in
+ * shared memory (tier 5, distances up to kLongSmemDistance) or in the CTA's
+ * global scratch (tier 6).  Each step also writes -1 two cells beyond its
+ * range, so the next step reads the reference's sentinel there.  The 2-bit
+ * backtrace store is in global scratch, row d holding ceil((2d+1)/32) 64-bit
+ * entries (low and high operation bits of 32 diagonals). */
+
+/* first entry of row d (d >= 1) of the long-tier backtrace store:
+ * sum over e in [1, d-1] of ceil((2e+1)/32) = floor(e/16) + 1 */
+__host__ __device__ __forceinline__ uint64_t long_row(int d)
+{
+    const uint64_t n = (uint64_t)(d - 1);
+    const uint64_t a = n >> 4, b = n & 15u;
+    return n + 8u * a * (a >= 1 ? a - 1 : 0) + a * (b + 1);
+}
+
+template <bool GLOBAL_WF>
+__global__ void __launch_bounds__(kLongThreads) long_kernel(AlignLaunch A)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    constexpr int kW = kLongThreads / 32;
+    const TierShape& sh = A.chain.shape[A.tier];
+    const int dlim = sh.dlim;
+    const int W = 2 * dlim + 5; /* entries per wavefront buffer, centre dlim + 2 */
+    const int lane = (int)(threadIdx.x & 31u), warp = (int)(threadIdx.x >> 5);
+    const uint32_t seq_words = sh.seq_words;
+    uint2* QP = reinterpret_cast<uint2*>(smem);
+    uint2* QT = QP + seq_words;
+    unsigned char* slab = sh.scratch + (size_t)blockIdx.x * sh.slab;
+    uint2* ops = reinterpret_cast<uint2*>(slab);
+    const uint64_t ops_entries = long_row(dlim + 1);
+    uint8_t* chain = slab + ops_entries * 8u;
+    int* runs = reinterpret_cast<int*>(chain + ((dlim + 16) & ~15));
+    int* wf;
+    if constexpr (GLOBAL_WF)
+        wf = runs + ((dlim + 4) & ~3);
+    else
+        wf = reinterpret_cast<int*>(QT + seq_words);
+    int* bufA = wf + dlim + 2;     /* centred */
+    int* bufB = wf + W + dlim + 2;
+
+    const uint32_t count = A.work_count ? min(*A.work_count, A.n_work) : A.n_work;
+    for (uint32_t item = blockIdx.x; item < count; item += gridDim.x) {
+        const uint32_t pi = A.work ? A.work[item] : item;
+        const PairRef pr = get_pair(A.L, pi);
+        const uint32_t mx = max(pr.plen, pr.tlen);
+        int state = !pr.in_range ? ST_RANGE : (mx > A.max_len || mx > 16u * seq_words) ? ST_TOOLONG : ST_RUN;
+        const int plen = state == ST_RUN ? (int)pr.plen : 0, tlen = state == ST_RUN ? (int)pr.tlen : 0;
+        const int kt = tlen - plen;
+        if (warp == 0) load_packed<32, 4>(pr.p, (uint32_t)plen, QP, lane, kFull);
+        if (warp == 1) load_packed<32, 4>(pr.t, (uint32_t)tlen, QT, lane, kFull);
+        __syncthreads();
+        int D = 0;
+        if (state == ST_RUN) {
+            /* score 0 (src/kernels.cu:249-258) */
+            if (threadIdx.x == 0) {
+                bufA[0] = extend_lane(QP, QT, plen, tlen, 0, 0);
+                bufA[1] = bufA[-1] = bufA[2] = bufA[-2] = -1;
+            }
+            __syncthreads();
+            int* prev = bufA;
+            int* next = bufB;
+            if (!(kt == 0 && prev[0] == tlen)) {
+                for (int d = 1;; ++d) {
+                    if (A.max_distance > 0 && d > A.max_distance) { state = ST_OVERMAX; break; }
+                    if (d > dlim) { state = ST_OVERFLOW; break; }
+                    const int ncell = 2 * d + 1;
+                    const int nchunk = (ncell + 31) >> 5;
+                    uint2* row = ops + long_row(d);
+                    for (int q = warp; q < nchunk; q += kW) {
+                        const int i = 32 * q + lane;
+                        const int k = i - d;
+                        const bool valid = i < ncell;
+                        int m = 0;
+                        if (valid) {
+                            const int del_p = (int)(((unsigned)prev[k + 1]) << 2) | kOpDel;
+                            const int sub_p = (int)(((unsigned)(prev[k] + 1)) << 2) | kOpSub;
+                            const int ins_p = (int)(((unsigned)(prev[k - 1] + 1)) << 2) | kOpIns;
+                            m = max(max(del_p, sub_p), ins_p);
+                            next[k] = extend_lane(QP, QT, plen, tlen, k, m >> 2);
+                        }
+                        const unsigned lo = __ballot_sync(kFull, m & 1);
+                        const unsigned hi = __ballot_sync(kFull, m & 2);
+                        if (lane == 0) row[q] = make_uint2(lo, hi);
+                    }
+                    if (threadIdx.x == 0) next[d + 1] = next[-d - 1] = next[d + 2] = next[-d - 2] = -1;
+                    __syncthreads();
+                    if (kt >= -d && kt <= d && next[kt] == tlen) { D = d; break; }
+                    int* t = prev; prev = next; next = t;
+                }
+            }
+            if (state == ST_RUN) state = ST_DONE;
+        }
+        if (state == ST_DONE && warp == 0) {
+            /* backtrace, 32 rows per round: lane r fetches row s-r's entries
+             * around the walk (it moves 0-2 positions down per row), then
+             * all lanes walk them through shuffles */
+            int p = kt + D;
+            int s = D;
+            bool ok = true;
+            while (s >= 1 && ok) {
+                const int ctop = p >> 5;
+                const int sr = s - lane;
+                uint2 e0 = make_uint2(0, 0), e1 = e0, e2 = e0;
+                if (sr >= 1) {
+                    const uint2* rw = ops + long_row(sr);
+                    const int last = (2 * sr) >> 5;
+                    if (ctop - 2 >= 0 && ctop - 2 <= last) e0 = rw[ctop - 2];
+                    if (ctop - 1 >= 0 && ctop - 1 <= last) e1 = rw[ctop - 1];
+                    if (ctop <= last) e2 = rw[ctop];
+                }
+                const int steps = min(32, s);
+                for (int r = 0; r < steps; ++r) {
+                    const int sel = (p >> 5) - (ctop - 2);
+                    const uint2 mine = sel == 0 ? e0 : (sel == 1 ? e1 : e2);
+                    const unsigned lo = __shfl_sync(kFull, mine.x, r);
+                    const unsigned hi = __shfl_sync(kFull, mine.y, r);
+                    const int bit = p & 31;
+                    const int op = (int)(((lo >> bit) & 1u) | (((hi >> bit) & 1u) << 1));
+                    const int row = s - r;
+                    if (op == 0 || sel < 0 || sel > 2 || p < 0 || p > 2 * row) { ok = false; break; }
+                    if (lane == 0) chain[row - 1] = (uint8_t)op;
+                    p += op - 3;
+                }
+                s -= steps;
+            }
+            if (ok && p != 0) ok = false;
+            if (!ok) state = ST_BADWALK;
+            __syncwarp();
+            if (state == ST_DONE) {
+                int8_t* dst = A.cigar_stride ? A.cigar + (size_t)pi * A.cigar_stride : nullptr;
+                const int len = replay_chain<32>(QP, QT, plen, tlen, chain, D, runs, dst, dst ? A.cigar_stride : 0u,
+                                                 lane, 0, kFull);
+                if (lane == 0) {
+                    if (dst && (uint32_t)len < A.cigar_stride) dst[len] = 0;
+                    A.dist[pi] = D;
+                    if (A.status)
+                        A.status[pi] = (uint32_t)len > A.cigar_stride ? (uint8_t)WFE_PAIR_CIGAR_TRUNCATED
+                                                                      : (uint8_t)WFE_PAIR_OK;
+                }
+            }
+        }
+        if (threadIdx.x == 0 && state != ST_DONE && state != ST_IDLE) {
+            if (state == ST_OVERFLOW && A.retry) {
+                const uint32_t s = atomicAdd(A.retry_count, 1u);
+                A.retry[s] = pi;
+                if (A.passed_total) atomicAdd(A.passed_total, 1ull);
+            } else {
+                A.dist[pi] = state == ST_OVERMAX ? A.max_distance + 1 : -1;
+                if (A.status)
+                    A.status[pi] = state == ST_OVERMAX  ? (uint8_t)WFE_PAIR_OVER_MAX_DISTANCE
+                                   : state == ST_BADWALK ? (uint8_t)WFE_PAIR_BAD_HISTORY
+                                   : state == ST_RANGE   ? (uint8_t)WFE_PAIR_OUT_OF_RANGE
+                                                         : (uint8_t)WFE_PAIR_TOO_LONG;
+                if (A.cigar_stride) A.cigar[(size_t)pi * A.cigar_stride] = 0;
+            }
+        }
+        __syncthreads();
+    }
+
+    if (A.chain.cta_done) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            const unsigned t = atomicAdd(A.chain.cta_done + A.tier, 1u);
+            if (t == gridDim.x - 1u) {
+                __threadfence();
+                const uint32_t cnt = *reinterpret_cast<volatile const uint32_t*>(A.retry_count);
+                if (cnt > 0u && A.tier < A.chain.last_tier) launch_next_tier(A, cnt);
+            }
+        }
+    }
+}
+
 const TierInfo kTiers[kNumTiers] = {
     {T0::G, T0::J, T0::DCAP, T0::SMEM_OPS},
     {T1::G, T1::J, T1::DCAP, T1::SMEM_OPS},
     {T2::G, T2::J, T2::DCAP, T2::SMEM_OPS},
     {T3::G, T3::J, T3::DCAP, T3::SMEM_OPS},
     {T4::G, T4::J, T4::DCAP, T4::SMEM_OPS},
+    {kLongThreads, 0, kLongSmemDistance, false},
+    {kLongThreads, 0, 0x7fffffff, false},
 };
 
 template <class T>
@@ -482,6 +677,51 @@ size_t tier_scratch_bytes(int tier, int grid)
     }
 }
 
+uint64_t long_slab_bytes(int dlim, bool global_wavefront)
+{
+    uint64_t b = long_row(dlim + 1) * 8u;              /* backtrace store */
+    b += (uint64_t)((dlim + 16) & ~15);                 /* chain */
+    b += 4u * (uint64_t)((dlim + 4) & ~3);              /* runs */
+    if (global_wavefront) b += 8u * (uint64_t)(2 * dlim + 5); /* two wavefront buffers */
+    return (b + 255u) & ~uint64_t(255);
+}
+
+namespace {
+
+template <bool GWF>
+TierShape long_shape_of(uint32_t max_len, int sm_count)
+{
+    TierShape sh{};
+    const int dlim = GWF ? (int)max_len : (int)std::min<uint32_t>(max_len, kLongSmemDistance);
+    const uint32_t sw = seq_words_for(max_len);
+    const size_t smem = 16u * (size_t)sw + (GWF ? 0u : 8u * (size_t)(2 * dlim + 5));
+    if (smem > 227u * 1024u) return sh;
+    if (cudaFuncSetAttribute(long_kernel<GWF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return sh;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, long_kernel<GWF>, kLongThreads, smem) != cudaSuccess)
+        return sh;
+    sh.grid = std::max(1, nb) * sm_count;
+    sh.smem = (uint32_t)smem;
+    sh.seq_words = sw;
+    sh.dlim = dlim;
+    sh.slab = long_slab_bytes(dlim, GWF);
+    return sh;
+}
+
+template <bool GWF>
+cudaError_t launch_long(const AlignLaunch& a, int grid, cudaStream_t s)
+{
+    const TierShape& sh = a.chain.shape[a.tier];
+    if (!sh.scratch || sh.smem == 0) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(long_kernel<GWF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem);
+    if (e != cudaSuccess) return e;
+    long_kernel<GWF><<<grid, kLongThreads, sh.smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
 TierShape tier_shape(int tier, uint32_t max_len, uint32_t cigar_stride, int sm_count)
 {
     switch (tier) {
@@ -490,20 +730,15 @@ TierShape tier_shape(int tier, uint32_t max_len, uint32_t cigar_stride, int sm_c
     case 2: return shape_of<T2>(max_len, cigar_stride, sm_count);
     case 3: return shape_of<T3>(max_len, cigar_stride, sm_count);
     case 4: return shape_of<T4>(max_len, cigar_stride, sm_count);
+    case 5: return long_shape_of<false>(max_len, sm_count);
+    case 6: return max_len > (uint32_t)kLongSmemDistance ? long_shape_of<true>(max_len, sm_count) : TierShape{};
     default: return TierShape{};
     }
 }
 
 int tier_grid(int tier, uint32_t max_len, uint32_t cigar_stride, int sm_count)
 {
-    switch (tier) {
-    case 0: return grid_of<T0>(max_len, cigar_stride, sm_count);
-    case 1: return grid_of<T1>(max_len, cigar_stride, sm_count);
-    case 2: return grid_of<T2>(max_len, cigar_stride, sm_count);
-    case 3: return grid_of<T3>(max_len, cigar_stride, sm_count);
-    case 4: return grid_of<T4>(max_len, cigar_stride, sm_count);
-    default: return 0;
-    }
+    return tier_shape(tier, max_len, cigar_stride, sm_count).grid;
 }
 
 cudaError_t launch_tier(int tier, const AlignLaunch& a, int grid, cudaStream_t s)
@@ -515,6 +750,8 @@ cudaError_t launch_tier(int tier, const AlignLaunch& a, int grid, cudaStream_t s
     case 2: return launch<T2>(a, grid, s);
     case 3: return launch<T3>(a, grid, s);
     case 4: return launch<T4>(a, grid, s);
+    case 5: return launch_long<false>(a, grid, s);
+    case 6: return launch_long<true>(a, grid, s);
     default: return cudaErrorInvalidValue;
     }
 }

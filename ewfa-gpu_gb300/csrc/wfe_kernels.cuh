@@ -18,7 +18,12 @@ struct TierInfo {
     bool ops_in_smem;
 };
 
-constexpr int kNumTiers = 5;
+/* Tiers 0-4 are register tiers (one pair per group of G lanes); tiers 5
+ * and 6 give each pair a whole CTA with the wavefront in shared (5) or
+ * global (6) memory and have no distance limit of their own. */
+constexpr int kNumTiers = 7;
+constexpr int kLongThreads = 256;
+constexpr int kLongSmemDistance = 2047; /* largest distance with the wavefront in shared memory */
 const TierInfo& tier_info(int t);
 
 /* Launch shape of one tier, for launches made on the device. */
@@ -27,7 +32,15 @@ struct TierShape {
     uint32_t smem;      /* dynamic shared memory per CTA */
     uint32_t seq_words; /* 16-base words per sequence in shared memory */
     uint32_t gbytes;    /* shared memory per group */
+    int dlim;           /* tiers 5-6: largest distance the tier computes */
+    uint64_t slab;      /* tiers 5-6: bytes of global scratch per CTA */
+    unsigned char* scratch; /* tiers 5-6: grid * slab bytes */
 };
+
+/* Global scratch of one CTA of tiers 5-6 for distances up to dlim: 2-bit
+ * backtrace store (rows 1..dlim, a 64-bit entry per 32 diagonals),
+ * operation chain, runs, and for tier 6 the two wavefront buffers. */
+uint64_t long_slab_bytes(int dlim, bool global_wavefront);
 
 /* The tier chain of one batch.  Each tier kernel's last CTA launches the
  * next tier as a tail launch when it handed any pair on, so no launch is

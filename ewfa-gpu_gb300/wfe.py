@@ -33,6 +33,8 @@ SYMBOLS = [
     "wfe_create", "wfe_destroy", "wfe_strerror", "wfe_last_cuda_error", "wfe_get_stats",
     "wfe_reset_stats", "wfe_align", "wfe_align_strided", "wfe_align_device", "wfe_pack_device",
     "wfe_cigar_from_history_device", "wfe_format_cigar", "wfe_check_cigar", "wfe_align_device_noalloc",
+    "wfe_read_pair_file", "wfe_free_pair_file", "wfe_host_alloc", "wfe_host_free", "wfe_device_count",
+    "wfe_device_name",
 ]
 NOALLOC_MAX_DISTANCE = 271
 NOALLOC_SCRATCH_BYTES = 16 << 20
@@ -54,6 +56,11 @@ class Stats(C.Structure):
                 ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("tier_entered", C.c_uint64 * 8),
                 ("tier_passed", C.c_uint64 * 8), ("tier_launches", C.c_uint64 * 8),
                 ("tier_ms", C.c_double * 8), ("mapped_batches", C.c_uint64)]
+
+
+class PairFileC(C.Structure):
+    _fields_ = [("ascii", C.c_void_p), ("ascii_bytes", C.c_size_t), ("pairs", C.c_void_p), ("n", C.c_size_t),
+                ("longest", C.c_uint32), ("pinned", C.c_int)]
 
 
 class GenConfig(C.Structure):
@@ -95,6 +102,14 @@ def load() -> C.CDLL:
     L.wfe_format_cigar.restype = sz
     L.wfe_check_cigar.argtypes = [C.c_char_p, u32, C.c_char_p, u32, vp, sz, C.POINTER(i32)]
     L.wfe_align_device_noalloc.argtypes = [vp, vp, sz, u32, i32, vp, vp, u32, vp, vp]
+    L.wfe_read_pair_file.argtypes = [C.c_char_p, sz, C.c_int, C.c_int, C.POINTER(PairFileC), C.c_char_p, sz]
+    L.wfe_free_pair_file.argtypes = [C.POINTER(PairFileC)]
+    L.wfe_free_pair_file.restype = None
+    L.wfe_host_alloc.argtypes = [C.POINTER(C.c_void_p), sz]
+    L.wfe_host_free.argtypes = [vp]
+    L.wfe_host_free.restype = None
+    L.wfe_device_count.argtypes = [C.POINTER(C.c_int)]
+    L.wfe_device_name.argtypes = [C.c_int, C.c_char_p, sz, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     for name in SYMBOLS:
         getattr(L, name)
     _lib = L
@@ -177,6 +192,24 @@ def generate_file(path: str, n: int, len_min: int, len_max: int | None = None, p
                     p_max if p_max is not None else p_min)
     if gen_lib().wfe_gen_file(C.byref(cfg), first, n, path.encode()) != 0:
         raise RuntimeError(f"could not write {path}")
+
+
+def read_pair_file(path: str, max_pairs: int = 1 << 62, nthreads: int = 0, pin: bool = False):
+    """wfe_read_pair_file: (ascii uint8[], pairs PAIR_DTYPE[], longest) copied
+    out of the library's buffers."""
+    f = PairFileC()
+    err = C.create_string_buffer(256)
+    rc = load().wfe_read_pair_file(path.encode(), max_pairs, nthreads or (os.cpu_count() or 1), int(pin),
+                                   C.byref(f), err, 256)
+    if rc != OK:
+        raise WfeError(rc, err.value.decode() or "wfe_read_pair_file")
+    try:
+        ascii = np.ctypeslib.as_array((C.c_uint8 * (f.ascii_bytes + 64)).from_address(f.ascii)).copy()
+        pairs = np.ctypeslib.as_array((C.c_uint8 * (24 * f.n)).from_address(f.pairs)).copy().view(PAIR_DTYPE) \
+            if f.n else np.zeros(0, PAIR_DTYPE)
+        return ascii, pairs, f.longest
+    finally:
+        load().wfe_free_pair_file(C.byref(f))
 
 
 def pairs_from_list(seqs):

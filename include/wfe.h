@@ -257,6 +257,30 @@ int wfe_device_name(int device, char* name, size_t cap, int* cc_major, int* cc_m
 int wfe_host_alloc(void** p, size_t bytes);
 void wfe_host_free(void* p);
 
+/* ---- pair files ------------------------------------------------------------ */
+
+/* A pair file read into memory: the file's bytes and one descriptor per pair
+ * pointing into them (no sequence byte copied). */
+typedef struct wfe_pair_file {
+    char* ascii;        /* the file's bytes (+64 zero bytes) */
+    size_t ascii_bytes; /* file size */
+    wfe_pair* pairs;    /* n descriptors into ascii */
+    size_t n;           /* pairs read */
+    uint32_t longest;   /* longest pattern or text */
+    int pinned;         /* ascii and pairs are page-locked (read in place by wfe_align) */
+} wfe_pair_file;
+
+/* Read up to max_pairs pairs of a ">pattern" / "<text" file (one sequence
+ * per line, '\n' or "\r\n" endings) with nthreads threads; pin = 1 asks for
+ * page-locked buffers.  Replaces SequenceReader::read_n_alignments
+ * (utils/sequence_reader.cu:108-201), which copies every sequence into a
+ * 2*l+pad slot and drops the last base of a final line without '\n'.
+ * On a format error returns WFE_ERR_INVALID_ARGUMENT and writes the message
+ * into err (err_cap bytes). */
+int wfe_read_pair_file(const char* path, size_t max_pairs, int nthreads, int pin,
+                       wfe_pair_file* out, char* err, size_t err_cap);
+void wfe_free_pair_file(wfe_pair_file* f);
+
 /* ---- host CIGAR utilities ---------------------------------------------- */
 
 /* Text of one encoded CIGAR.  compat = 0: run-length form, e.g.

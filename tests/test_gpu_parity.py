@@ -359,3 +359,31 @@ def test_pinned_strided_layout():
     np.testing.assert_array_equal(got[0], want[0])
     assert_same_cigars(got[1], want[1])
     compare_with_oracle(ascii, pairs, 152, *want)
+
+
+def test_long_tiers_without_distance_limit():
+    """Unrelated random pairs (distance about half the length) reach the
+    CTA-per-pair tiers: shared-memory wavefront up to distance 2047 (tier
+    5), global-memory wavefront beyond (tier 6)."""
+    rng = np.random.default_rng(5)
+    seqs = []
+    def rand(L):
+        return np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, L)].tobytes()
+
+    for L in [700, 900, 1200, 1500, 2000, 2600] * 3 + [4300, 4700]:
+        seqs.append((rand(L), rand(L + int(rng.integers(-30, 30)))))
+    # and a few near-identical long pairs, so tiers 5-6 also see long runs
+    for L in [3000, 4900]:
+        t = rand(L)
+        p = bytearray(t)
+        for j in rng.choice(L, 40, replace=False):
+            p[j] = b"ACGT"[(b"ACGT".index(p[j]) + 1) % 4]
+        seqs.append((bytes(p), t))
+    ascii, pairs = wfe.pairs_from_list(seqs)
+    with wfe.Context(max_seq_len=5000, cigar_stride=12000) as ctx:
+        dist, cg, st = ctx.align(ascii, pairs)
+        stats = ctx.stats()
+    assert dist.max() > 2047
+    assert stats["tier_passed"][4] > 0 and stats["tier_passed"][5] > 0, stats
+    assert (st == 0).all()
+    compare_with_oracle(ascii, pairs, 12000, dist, cg, st)
