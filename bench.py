@@ -57,6 +57,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=["short", "mixed"], default="short",
+                    help="short: the short-read throughput workload (the metric's configuration); "
+                         "mixed: uneven lengths, plain fixed-shape launches vs length buckets")
+    ap.add_argument("--pairs", type=int, default=0, help="mixed workload: number of pairs (default 2,000,000)")
     ap.add_argument("--profile-batch", type=int, default=0,
                     help="profiling case: align this many pairs of the workload as ONE batch, twice "
                          "(a warm-up chain, then the chain to capture), and exit")
@@ -83,6 +87,81 @@ def run_profile_case(n: int) -> int:
     print(json.dumps({"profile_batch": n, "device_MiB": round(mb, 1), "tier_launches": launches,
                       "status_ok": bool((d_status.cpu().numpy() == 0).all())}))
     return 0
+
+
+MIXED_PAIRS, MIXED_LMIN, MIXED_LMAX, MIXED_PMIN, MIXED_PMAX, MIXED_SEED = 2_000_000, 100, 10_000, 0.01, 0.15, 4
+MIXED_BUCKETS = [256, 512, 1024, 2048, 4096, 11_000]
+
+
+def run_mixed(args) -> int:
+    """Uneven sizes: lengths log-uniform in [100, 10,000], edit probability
+    uniform in [0.01, 0.15].  The same device-resident pairs are aligned
+    (1) with the plain fixed-shape launches: one launch shape for every pair,
+        sized for the longest sequence, and
+    (2) with length buckets: pairs sorted by length on the device, each
+        bucket aligned with shapes sized to it, first tiers chosen by the
+        autotuner on a sample, and
+    (3) as (2) with distance prediction: every pair starts at the tier its
+        128-base prefix distance, extrapolated to its length, calls for,
+    in batches of 100,000; all must give the same distances and CIGARs."""
+    import torch
+    torch.cuda.set_device(0)
+    n = args.pairs or MIXED_PAIRS
+    ascii, pairs = wfe.generate(n, MIXED_LMIN, MIXED_LMAX, p_min=MIXED_PMIN, p_max=MIXED_PMAX, seed=MIXED_SEED)
+    max_len = int(max(pairs["p_len"].max(), pairs["t_len"].max()))
+    max_seq = MIXED_BUCKETS[-1]
+    assert max_len <= max_seq
+    stride = 4096
+    d_ascii = torch.from_numpy(ascii).cuda()
+    d_pairs = torch.from_numpy(pairs.view(np.uint8)).cuda()
+    outs = {}
+    res = {}
+    cache = os.path.join(tempfile.gettempdir(), "wfe_autotune.jsonl")
+    modes = ("plain", "bucketed", "predicted")
+    for mode in modes:
+        d_dist = torch.zeros(n, dtype=torch.int32, device="cuda")
+        d_cg = torch.zeros(n * stride, dtype=torch.int8, device="cuda")
+        d_st = torch.full((n,), 255, dtype=torch.uint8, device="cuda")  # 255: never written
+        with wfe.Context(max_seq_len=max_seq, batch_size=BATCH, cigar_stride=stride,
+                         flags=wfe.FLAG_KERNEL_TIMING) as ctx:
+            tiers = None
+            t_tune = 0.0
+            if mode != "plain":
+                t0 = time.perf_counter()
+                tiers = ctx.autotune(d_ascii, d_pairs, n, MIXED_BUCKETS, cache, predict=mode == "predicted")
+                t_tune = time.perf_counter() - t0
+            s = torch.cuda.Stream()
+            ctx.align_device(d_ascii, d_pairs, min(n, BATCH), max_seq, d_dist, d_cg, d_st, s)  # warm-up
+            torch.cuda.synchronize()
+            ctx.reset_stats()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            ctx.align_device(d_ascii, d_pairs, n, max_seq, d_dist, d_cg, d_st, s)
+            e1.record(s)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            st = ctx.stats()
+            res[mode] = {"seconds": ms / 1e3, "alignments_per_s": n / (ms / 1e3), "first_tiers": tiers,
+                         "tune_seconds": round(t_tune, 3), "kernel_launches": st["kernel_launches"],
+                         "tier_launches": st["tier_launches"][:7], "tier_passed": st["tier_passed"][:7]}
+        outs[mode] = (d_dist.cpu().numpy(), d_st.cpu().numpy(), d_cg)
+    same_dist = all(np.array_equal(outs["plain"][0], outs[m][0]) for m in modes)
+    same_status = all(np.array_equal(outs["plain"][1], outs[m][1]) for m in modes)
+    same_status = same_status and all(torch.equal(outs["plain"][2], outs[m][2]) for m in modes)  # CIGAR slots
+    ok_status = all(bool((outs[m][1] == 0).all()) for m in modes)
+    dist = outs["plain"][0]
+    line = {"metric": "alignments/sec", "workload": "mixed", "pairs": n, "unit": "alignments/s",
+            "config": {"lengths": f"log-uniform [{MIXED_LMIN}, {MIXED_LMAX}]",
+                       "edit_prob": f"uniform [{MIXED_PMIN}, {MIXED_PMAX}]", "seed": MIXED_SEED, "batch": BATCH,
+                       "buckets": MIXED_BUCKETS, "cigar_stride": stride},
+            **res,
+            "speedup": {m: res["plain"]["seconds"] / res[m]["seconds"] for m in modes[1:]},
+            "gcups": {m: n * float(np.mean(pairs["p_len"].astype(np.float64) * pairs["t_len"])) /
+                      res[m]["seconds"] / 1e9 for m in modes},
+            "identical_results": same_dist and same_status, "all_ok": ok_status,
+            "distance": {"mean": float(dist.mean()), "max": int(dist.max())}}
+    print(json.dumps(line))
+    return 0 if same_dist and same_status and ok_status else 1
 
 
 def dist_env():
@@ -271,6 +350,8 @@ def main():
     args = parse()
     if args.profile_batch:
         return run_profile_case(args.profile_batch)
+    if args.workload == "mixed":
+        return run_mixed(args)
     if args.impl == "reference":
         return run_reference(args)
     import torch
@@ -323,6 +404,7 @@ def main():
     ms_max = reduce_max(ms, world, device)
     st = ctx.stats()
     value = world * args.steps * BATCH / (ms_max / 1e3)
+    cells_per_pair = float(np.mean(pairs["p_len"].astype(np.float64) * pairs["t_len"]))
 
     # algorithmic bytes of one batch: ASCII read once, descriptors, and the
     # distance, status and CIGAR bytes (with terminator) written
@@ -402,6 +484,8 @@ def main():
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": f"tier_kernel tier {top}", "alg_bytes_per_launch": alg_bytes,
                          "launch_ms": launch_ms},
+            "gcups": {"value": value * cells_per_pair / 1e9,
+                      "definition": "equivalent DP cell updates: sum of p_len * t_len per second / 1e9"},
             "cpu_baseline": base,
             "ref_cuda": ref_cuda,
             "e2e": e2e,

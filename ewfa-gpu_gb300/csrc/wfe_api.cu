@@ -12,6 +12,9 @@
  */
 #include <algorithm>
 #include <cstdio>
+#include <fstream>
+#include <sstream>
+#include <string>
 #include <cstdlib>
 #include <cstring>
 #include <new>
@@ -37,7 +40,8 @@ struct Stage {
     int8_t* d_cigar = nullptr;
     uint8_t* d_status = nullptr;
     uint32_t* d_lists = nullptr;  /* two retry lists of batch_size entries */
-    uint32_t* d_counts = nullptr; /* one retry counter per tier */
+    uint32_t* d_counts = nullptr; /* per bucket: list counts, finished CTAs, work counters */
+    uint16_t* d_pred = nullptr;   /* predicted prefix distances */
     char* h_stage = nullptr;      /* pinned gather buffer for scattered inputs */
     wfe_pair* h_pairs = nullptr;  /* pinned descriptors of a gathered batch */
 };
@@ -51,21 +55,36 @@ struct TimedLaunch {
     cudaEvent_t start, stop;
 };
 
+/* How the pairs of one length bucket are aligned: the first tier and the
+ * launch shape of every tier for sequences up to max_len. */
+struct BucketPlan {
+    uint32_t max_len = 0;
+    int first_tier = 0;
+    int last_tier = 0;
+    TierShape shape[kNumTiers] = {};
+};
+
 struct wfe_ctx {
     wfe_config cfg{};
     int sm_count = 0;
-    int first_tier = 0;
-    int last_tier = 0;      /* 5, or 6 when sequences can be longer than kLongSmemDistance */
-    int grid[kNumTiers] = {};
-    TierShape shape[kNumTiers] = {};
-    unsigned char* d_ops_scratch = nullptr;
+    int nbuckets = 1;
+    BucketPlan bucket[kMaxBuckets];
+    bool predict = false;                      /* route pairs by predicted distance */
+    int scratch_ctas[kNumTiers] = {};          /* CTAs whose global scratch is allocated */
+    unsigned char* d_ops_scratch = nullptr;    /* tiers 3-4 backtrace stores */
     size_t ops_scratch_bytes = 0;
-    unsigned long long* d_passed = nullptr;   /* pairs each tier handed on, running total */
-    unsigned long long* d_launched = nullptr; /* tier launches made on the device */
+    unsigned char* d_long_scratch[kNumTiers] = {}; /* tiers 5-6 slabs */
+    uint64_t long_slab[kNumTiers] = {};
+    unsigned long long* d_passed = nullptr;    /* pairs each tier handed on, running total */
+    unsigned long long* d_launched = nullptr;  /* tier launches made on the device */
+    unsigned long long* d_bucket_total = nullptr; /* pairs classified into each bucket */
+    uint32_t* h_launch_error = nullptr;        /* host-mapped: bit t, a device-side launch of tier t failed */
+    uint32_t* d_launch_error = nullptr;        /* its device address */
+    uint64_t single_entered[kNumTiers] = {};   /* first-tier entries of one-bucket batches */
     Stage st[kStages];
     int last_cuda_error = 0;
     wfe_stats stats{};
-    std::vector<TimedLaunch> timed;      /* launches whose events are not read yet */
+    std::vector<TimedLaunch> timed;            /* launches whose events are not read yet */
     std::vector<cudaEvent_t> event_pool;
 };
 
@@ -83,20 +102,39 @@ int fail_cuda(wfe_ctx* ctx, cudaError_t e)
         if (e_ != cudaSuccess) return fail_cuda((ctx), e_);        \
     } while (0)
 
+/* Device-side tier launches that failed (their pairs were left unaligned)
+ * since the last call, reported once as a CUDA launch failure.  Read after
+ * the work in question has completed. */
+int take_launch_error(wfe_ctx* ctx)
+{
+    volatile uint32_t* f = ctx->h_launch_error;
+    if (!f || *f == 0u) return WFE_OK;
+    *f = 0u;
+    return fail_cuda(ctx, cudaErrorLaunchFailure);
+}
+
 uint32_t default_cigar_stride(uint32_t max_seq_len)
 {
     /* src/wavefront.cuh:48-50: seq_len + (4 - seq_len % 4) */
     return max_seq_len + (4u - max_seq_len % 4u);
 }
 
-/* First tier by sequence length: short reads almost always finish in the
- * 8-lane tier; long reads start where their distances usually are. */
+/* First tier by sequence length, used until a policy says otherwise: short
+ * reads almost always finish in the 4-lane tier; long reads start where
+ * their distances usually are. */
 int default_first_tier(uint32_t max_len)
 {
     if (max_len <= 1200) return 0;
     if (max_len <= 2000) return 2;
     return 3;
 }
+
+/* per-stage counters, per bucket: the count of every tier's list, finished
+ * CTAs and work counters of every tier; per-stage lists: one per bucket and
+ * tier */
+constexpr size_t kChainWords = 3 * kNumTiers + 1;
+constexpr size_t kCountWords = kMaxBuckets * kChainWords;
+constexpr size_t kLists = (size_t)kMaxBuckets * kNumTiers;
 
 void free_stage(Stage& s)
 {
@@ -109,77 +147,163 @@ void free_stage(Stage& s)
     cudaFree(s.d_status);
     cudaFree(s.d_lists);
     cudaFree(s.d_counts);
+    cudaFree(s.d_pred);
     cudaFreeHost(s.h_stage);
     cudaFreeHost(s.h_pairs);
     if (s.stream) cudaStreamDestroy(s.stream);
     s = Stage();
 }
 
-/* Enqueue the alignment of work items 0..n-1 of one batch on stream s: the
- * first tier is launched here; each tier's last CTA launches the next tier
- * on the device, and only when it handed pairs on. */
-int run_chain(wfe_ctx* ctx, Stage& st, const Layout& L, uint32_t n, int32_t* dist, int8_t* cigar,
-              uint8_t* status, cudaStream_t s)
+/* Launch shapes of every tier for sequences up to max_len, within the
+ * scratch the context holds. */
+void plan_bucket(wfe_ctx* ctx, BucketPlan& b)
 {
-    if (n == 0) return WFE_OK;
     const wfe_config& c = ctx->cfg;
-    WFE_CUDA(ctx, cudaMemsetAsync(st.d_counts, 0, sizeof(uint32_t) * 2 * kNumTiers, s));
+    b.last_tier = b.max_len > (uint32_t)kLongSmemDistance ? 6 : 5;
+    for (int t = 0; t < kNumTiers; ++t) {
+        TierShape sh = tier_shape(t, b.max_len, c.cigar_stride, ctx->sm_count);
+        if (t >= 3 && sh.grid > 0) sh.grid = std::min(sh.grid, ctx->scratch_ctas[t]);
+        if (t >= 5 && sh.grid > 0) {
+            sh.slab = ctx->long_slab[t];
+            sh.scratch = ctx->d_long_scratch[t];
+        }
+        b.shape[t] = sh;
+    }
+}
+
+bool bucket_usable(const BucketPlan& b)
+{
+    for (int t = b.first_tier; t <= b.last_tier; ++t)
+        if (b.shape[t].grid <= 0) return false;
+    return true;
+}
+
+TimedLaunch* begin_timing(wfe_ctx* ctx, int t, cudaStream_t s, int* rc)
+{
+    *rc = WFE_OK;
+    if (!(ctx->cfg.flags & WFE_FLAG_KERNEL_TIMING)) return nullptr;
+    TimedLaunch tl{t, nullptr, nullptr};
+    for (cudaEvent_t* ev : {&tl.start, &tl.stop}) {
+        if (!ctx->event_pool.empty()) {
+            *ev = ctx->event_pool.back();
+            ctx->event_pool.pop_back();
+        } else if (cudaEventCreate(ev) != cudaSuccess) {
+            *rc = WFE_ERR_CUDA;
+            return nullptr;
+        }
+    }
+    cudaEventRecord(tl.start, s);
+    ctx->timed.push_back(tl);
+    return &ctx->timed.back();
+}
+
+/* Launch the first tier of one bucket's chain over `work` (NULL: pairs
+ * 0..n-1); the last CTA of every tier starts the next tier with work, on the
+ * device. */
+int launch_bucket(wfe_ctx* ctx, Stage& st, const BucketPlan& bp, int bucket_index, int first_tier,
+                  const Layout& L, bool listed, uint32_t n, int32_t* dist, int8_t* cigar, uint8_t* status,
+                  cudaStream_t s)
+{
+    const wfe_config& c = ctx->cfg;
     const uint32_t B = c.batch_size;
-    const int t = ctx->first_tier;
+    const int t = first_tier;
+    uint32_t* words = st.d_counts + (size_t)bucket_index * kChainWords;
+    uint32_t* lists = st.d_lists + (size_t)bucket_index * kNumTiers * B;
     AlignLaunch a{};
     a.L = L;
-    a.work = nullptr;
-    a.work_count = nullptr;
+    a.work = listed ? lists + (size_t)t * B : nullptr;
+    a.work_count = listed ? words + t : nullptr;
     a.n_work = n;
     a.dist = dist;
     a.cigar = cigar;
     a.cigar_stride = c.cigar_stride;
     a.status = status;
     a.max_distance = c.max_distance;
-    a.max_len = c.max_seq_len;
-    a.retry_count = st.d_counts + t;
-    a.passed_total = ctx->d_passed + t;
+    a.max_len = bp.max_len;
     a.ops_scratch = ctx->d_ops_scratch;
     a.ops_scratch_bytes = ctx->ops_scratch_bytes;
     a.tier = t;
     /* a distance cap at or below a tier's capacity ends the chain there */
-    int last = ctx->last_tier;
+    int last = bp.last_tier;
     if (c.max_distance > 0)
-        for (int u = t; u < kNumTiers; ++u)
+        for (int u = t; u <= bp.last_tier; ++u)
             if (c.max_distance <= tier_info(u).dcap) { last = u; break; }
     a.chain.last_tier = last;
-    a.retry = t < last ? st.d_lists : nullptr;
-    for (int u = 0; u < kNumTiers; ++u) a.chain.shape[u] = ctx->shape[u];
-    a.chain.lists[0] = st.d_lists;
-    a.chain.lists[1] = st.d_lists + B;
-    a.chain.counts = st.d_counts;
-    a.chain.cta_done = st.d_counts + kNumTiers;
+    for (int u = 0; u < kNumTiers; ++u) {
+        a.chain.shape[u] = bp.shape[u];
+        a.chain.list[u] = lists + (size_t)u * B;
+    }
+    a.chain.counts = words;
+    a.chain.cta_done = words + kNumTiers + 1;
+    a.chain.work_next = words + 2 * kNumTiers + 1;
     a.chain.launched = ctx->d_launched;
-    const TierInfo& ti = tier_info(t);
-    const uint32_t per_cta = t >= 5 ? 1u : 4u * (32u / (uint32_t)ti.G);
-    int grid = (int)std::min<uint64_t>((uint64_t)ctx->grid[t], ((uint64_t)n + per_cta - 1) / per_cta);
+    a.chain.passed = ctx->d_passed;
+    a.chain.launch_error = ctx->d_launch_error;
+    a.retry = t < last ? a.chain.list[t + 1] : nullptr;
+    a.retry_count = words + t + 1;
+    a.passed_total = ctx->d_passed + t;
+    int grid = bp.shape[t].grid;
+    if (!listed) {
+        const uint32_t per_cta = t >= 5 ? 1u : 4u * (32u / (uint32_t)tier_info(t).G);
+        grid = (int)std::min<uint64_t>((uint64_t)grid, ((uint64_t)n + per_cta - 1) / per_cta);
+    }
     grid = std::max(grid, 1);
-    TimedLaunch tl{t, nullptr, nullptr};
-    const bool timing = (c.flags & WFE_FLAG_KERNEL_TIMING) != 0;
-    if (timing) {
-        for (cudaEvent_t* ev : {&tl.start, &tl.stop}) {
-            if (!ctx->event_pool.empty()) {
-                *ev = ctx->event_pool.back();
-                ctx->event_pool.pop_back();
-            } else {
-                WFE_CUDA(ctx, cudaEventCreate(ev));
-            }
-        }
-        WFE_CUDA(ctx, cudaEventRecord(tl.start, s));
-    }
+    int rc = WFE_OK;
+    TimedLaunch* tl = begin_timing(ctx, t, s, &rc);
+    if (rc != WFE_OK) return rc;
     WFE_CUDA(ctx, launch_tier(t, a, grid, s));
-    if (timing) {
-        WFE_CUDA(ctx, cudaEventRecord(tl.stop, s));
-        ctx->timed.push_back(tl);
-    }
+    if (tl) WFE_CUDA(ctx, cudaEventRecord(tl->stop, s));
     ctx->stats.kernel_launches++;
     ctx->stats.tier_launches[t]++;
-    ctx->stats.tier_entered[t] += n;
+    return WFE_OK;
+}
+
+/* Enqueue the alignment of pairs 0..n-1 of one batch on stream s: with one
+ * bucket and no prediction the batch goes straight to its first tier; else
+ * the pairs are routed on the device -- by length to a bucket whose launch
+ * shapes fit its longest sequence, and by predicted distance to a tier --
+ * and every bucket's chain runs from its first tier. */
+int run_chain(wfe_ctx* ctx, Stage& st, const Layout& L, uint32_t n, int32_t* dist, int8_t* cigar,
+              uint8_t* status, cudaStream_t s, const int* first_override = nullptr)
+{
+    if (n == 0) return WFE_OK;
+    const uint32_t B = ctx->cfg.batch_size;
+    WFE_CUDA(ctx, cudaMemsetAsync(st.d_counts, 0, sizeof(uint32_t) * kCountWords, s));
+    if (ctx->nbuckets == 1 && !ctx->predict) {
+        const BucketPlan& bp = ctx->bucket[0];
+        const int t = first_override ? first_override[0] : bp.first_tier;
+        ctx->single_entered[t] += n;
+        return launch_bucket(ctx, st, bp, 0, t, L, false, n, dist, cigar, status, s);
+    }
+    Buckets bk{};
+    bk.n = ctx->nbuckets;
+    for (int b = 0; b < ctx->nbuckets; ++b) {
+        bk.max_len[b] = ctx->bucket[b].max_len;
+        bk.first_tier[b] = first_override ? first_override[b] : ctx->bucket[b].first_tier;
+        bk.last_tier[b] = ctx->bucket[b].last_tier;
+    }
+    for (int t = 0; t < kNumTiers; ++t) bk.dcap[t] = tier_info(t).dcap;
+    /* predictions only move pairs of buckets that start below tier 5 */
+    bool predict = false;
+    for (int b = 0; b < ctx->nbuckets; ++b) predict |= ctx->predict && bk.first_tier[b] < 5;
+    if (predict) {
+        WFE_CUDA(ctx, launch_predict(L, n, ctx->cfg.max_seq_len, st.d_pred, ctx->bucket[0].shape[0].grid > 0
+                                         ? ctx->bucket[0].shape[0].grid : ctx->sm_count * 8, s));
+        ctx->stats.kernel_launches++;
+        bk.pred = st.d_pred;
+    }
+    bk.lists = st.d_lists;
+    bk.stride = B;
+    bk.counts = st.d_counts;
+    bk.count_stride = (uint32_t)kChainWords;
+    bk.totals = ctx->d_bucket_total;
+    WFE_CUDA(ctx, launch_classify(L, n, bk, s));
+    ctx->stats.kernel_launches++;
+    /* longest bucket first: its chains take longest */
+    for (int b = ctx->nbuckets - 1; b >= 0; --b) {
+        const int r = launch_bucket(ctx, st, ctx->bucket[b], b, bk.first_tier[b], L, true, n, dist, cigar, status, s);
+        if (r != WFE_OK) return r;
+    }
     return WFE_OK;
 }
 
@@ -227,49 +351,61 @@ int wfe_create(const wfe_config* cfg, wfe_ctx** out)
     wfe_config& c = ctx->cfg;
     if (c.batch_size == 0) c.batch_size = 100000;
     if (c.cigar_stride == 0) c.cigar_stride = default_cigar_stride(c.max_seq_len);
-    ctx->first_tier = default_first_tier(c.max_seq_len);
 
     auto bail = [&](cudaError_t err) {
         g_last_create_error = (int)err;
         for (auto& s : ctx->st) free_stage(s);
         cudaFree(ctx->d_ops_scratch);
         cudaFree(ctx->d_passed);
-        for (auto& sh : ctx->shape) cudaFree(sh.scratch);
+        cudaFreeHost(ctx->h_launch_error);
+        for (auto p : ctx->d_long_scratch) cudaFree(p);
         delete ctx;
         return err == cudaErrorMemoryAllocation ? WFE_ERR_OUT_OF_MEMORY : WFE_ERR_CUDA;
     };
 
     e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, c.device);
     if (e != cudaSuccess) return bail(e);
+    /* Global scratch is sized for the longest sequences (max_seq_len); a
+     * bucket of shorter sequences has more resident CTAs and uses at most
+     * the CTAs that scratch was sized for. */
     size_t scratch = 0;
-    ctx->last_tier = c.max_seq_len > (uint32_t)kLongSmemDistance ? 6 : 5;
-    for (int t = 0; t < kNumTiers; ++t) {
-        ctx->shape[t] = tier_shape(t, c.max_seq_len, c.cigar_stride, ctx->sm_count);
-        ctx->grid[t] = ctx->shape[t].grid;
-        if (ctx->grid[t] <= 0) { /* sequences too long for this tier's shared memory */
-            if (t >= ctx->first_tier && t <= ctx->last_tier) return bail(cudaErrorInvalidValue);
-            continue;
+    const int last = c.max_seq_len > (uint32_t)kLongSmemDistance ? 6 : 5;
+    for (int t = 0; t <= last; ++t) {
+        const TierShape sh = tier_shape(t, c.max_seq_len, c.cigar_stride, ctx->sm_count);
+        if (sh.grid <= 0) continue;
+        if (t == 3 || t == 4) {
+            ctx->scratch_ctas[t] = sh.grid;
+            scratch = std::max(scratch, tier_scratch_bytes(t, sh.grid));
+        } else if (t >= 5) {
+            /* a slab per resident CTA (backtrace store, chain, runs; tier 6
+             * also its wavefront), the grid trimmed to a budget */
+            const uint64_t budget = t == 5 ? (2ull << 30) : (8ull << 30);
+            const int grid = (int)std::min<uint64_t>((uint64_t)sh.grid, std::max<uint64_t>(1, budget / sh.slab));
+            ctx->scratch_ctas[t] = grid;
+            ctx->long_slab[t] = sh.slab;
+            if ((e = cudaMalloc(&ctx->d_long_scratch[t], (size_t)sh.slab * grid)) != cudaSuccess) return bail(e);
         }
-        if (t < 5) scratch = std::max(scratch, tier_scratch_bytes(t, ctx->grid[t]));
-    }
-    /* tiers 5-6: a scratch slab per resident CTA (backtrace store, chain,
-     * runs; tier 6 also its wavefront), the grid trimmed to a budget */
-    for (int t = 5; t <= ctx->last_tier; ++t) {
-        TierShape& sh = ctx->shape[t];
-        const uint64_t budget = t == 5 ? (2ull << 30) : (8ull << 30);
-        const uint64_t fit = std::max<uint64_t>(1, budget / sh.slab);
-        sh.grid = (int)std::min<uint64_t>((uint64_t)sh.grid, fit);
-        ctx->grid[t] = sh.grid;
-        if ((e = cudaMalloc(&sh.scratch, (size_t)sh.slab * sh.grid)) != cudaSuccess) return bail(e);
     }
     if (scratch) {
         e = cudaMalloc(&ctx->d_ops_scratch, scratch);
         if (e != cudaSuccess) return bail(e);
         ctx->ops_scratch_bytes = scratch;
     }
-    if ((e = cudaMalloc(&ctx->d_passed, sizeof(unsigned long long) * 2 * kNumTiers)) != cudaSuccess) return bail(e);
-    if ((e = cudaMemset(ctx->d_passed, 0, sizeof(unsigned long long) * 2 * kNumTiers)) != cudaSuccess) return bail(e);
+    ctx->nbuckets = 1;
+    ctx->bucket[0].max_len = c.max_seq_len;
+    ctx->bucket[0].first_tier = default_first_tier(c.max_seq_len);
+    plan_bucket(ctx, ctx->bucket[0]);
+    if (!bucket_usable(ctx->bucket[0])) return bail(cudaErrorInvalidValue); /* sequences too long for shared memory */
+
+    const size_t nctr = 2 * kNumTiers + kMaxBuckets;
+    if ((e = cudaMalloc(&ctx->d_passed, sizeof(unsigned long long) * nctr)) != cudaSuccess) return bail(e);
+    if ((e = cudaMemset(ctx->d_passed, 0, sizeof(unsigned long long) * nctr)) != cudaSuccess) return bail(e);
     ctx->d_launched = ctx->d_passed + kNumTiers;
+    ctx->d_bucket_total = ctx->d_passed + 2 * kNumTiers;
+    if ((e = cudaHostAlloc(&ctx->h_launch_error, sizeof(uint32_t), cudaHostAllocMapped)) != cudaSuccess)
+        return bail(e);
+    *ctx->h_launch_error = 0u;
+    if ((e = cudaHostGetDevicePointer(&ctx->d_launch_error, ctx->h_launch_error, 0)) != cudaSuccess) return bail(e);
     const size_t B = c.batch_size;
     for (auto& s : ctx->st) {
         s.ascii_cap = B * 2u * (size_t)c.max_seq_len + 64u;
@@ -281,10 +417,51 @@ int wfe_create(const wfe_config* cfg, wfe_ctx** out)
         if ((e = cudaMalloc(&s.d_dist, B * sizeof(int32_t))) != cudaSuccess) return bail(e);
         if ((e = cudaMalloc(&s.d_cigar, B * (size_t)c.cigar_stride + 16u)) != cudaSuccess) return bail(e);
         if ((e = cudaMalloc(&s.d_status, B)) != cudaSuccess) return bail(e);
-        if ((e = cudaMalloc(&s.d_lists, 2u * B * sizeof(uint32_t))) != cudaSuccess) return bail(e);
-        if ((e = cudaMalloc(&s.d_counts, sizeof(uint32_t) * 2 * kNumTiers)) != cudaSuccess) return bail(e);
+        /* a work list per length bucket and tier */
+        if ((e = cudaMalloc(&s.d_lists, kLists * B * sizeof(uint32_t))) != cudaSuccess) return bail(e);
+        if ((e = cudaMalloc(&s.d_counts, sizeof(uint32_t) * kCountWords)) != cudaSuccess) return bail(e);
+        if ((e = cudaMalloc(&s.d_pred, B * sizeof(uint16_t))) != cudaSuccess) return bail(e);
     }
     *out = ctx;
+    return WFE_OK;
+}
+
+int wfe_set_policy(wfe_ctx* ctx, uint32_t nbuckets, const uint32_t* bucket_max_len, const int32_t* first_tier,
+                   uint32_t flags)
+{
+    if (!ctx || nbuckets < 1 || nbuckets > (uint32_t)kMaxBuckets || !bucket_max_len) return WFE_ERR_INVALID_ARGUMENT;
+    if (flags & ~(uint32_t)WFE_POLICY_PREDICT) return WFE_ERR_INVALID_ARGUMENT;
+    BucketPlan plan[kMaxBuckets];
+    for (uint32_t b = 0; b < nbuckets; ++b) {
+        uint32_t m = bucket_max_len[b];
+        if (b + 1 == nbuckets) m = ctx->cfg.max_seq_len; /* the last bucket holds everything */
+        if (m == 0 || m > ctx->cfg.max_seq_len || (b > 0 && m <= plan[b - 1].max_len))
+            return WFE_ERR_INVALID_ARGUMENT;
+        plan[b].max_len = m;
+        const int32_t ft = first_tier ? first_tier[b] : -1;
+        if (ft >= kNumTiers) return WFE_ERR_INVALID_ARGUMENT;
+        plan[b].first_tier = ft < 0 ? default_first_tier(m) : ft;
+        plan_bucket(ctx, plan[b]);
+        if (plan[b].first_tier > plan[b].last_tier || !bucket_usable(plan[b])) return WFE_ERR_INVALID_ARGUMENT;
+    }
+    WFE_CUDA(ctx, cudaSetDevice(ctx->cfg.device));
+    for (auto& s : ctx->st) WFE_CUDA(ctx, cudaStreamSynchronize(s.stream));
+    ctx->nbuckets = (int)nbuckets;
+    for (uint32_t b = 0; b < nbuckets; ++b) ctx->bucket[b] = plan[b];
+    ctx->predict = (flags & WFE_POLICY_PREDICT) != 0;
+    return WFE_OK;
+}
+
+int wfe_get_policy(const wfe_ctx* ctx, uint32_t* nbuckets, uint32_t* bucket_max_len, int32_t* first_tier,
+                   uint32_t* flags)
+{
+    if (!ctx || !nbuckets) return WFE_ERR_INVALID_ARGUMENT;
+    *nbuckets = (uint32_t)ctx->nbuckets;
+    if (flags) *flags = ctx->predict ? WFE_POLICY_PREDICT : 0u;
+    for (int b = 0; b < ctx->nbuckets; ++b) {
+        if (bucket_max_len) bucket_max_len[b] = ctx->bucket[b].max_len;
+        if (first_tier) first_tier[b] = ctx->bucket[b].first_tier;
+    }
     return WFE_OK;
 }
 
@@ -298,7 +475,8 @@ void wfe_destroy(wfe_ctx* ctx)
     }
     cudaFree(ctx->d_ops_scratch);
     cudaFree(ctx->d_passed);
-    for (auto& sh : ctx->shape) cudaFree(sh.scratch);
+    cudaFreeHost(ctx->h_launch_error);
+    for (auto p : ctx->d_long_scratch) cudaFree(p);
     for (auto& t : ctx->timed) {
         cudaEventDestroy(t.start);
         cudaEventDestroy(t.stop);
@@ -321,15 +499,16 @@ int wfe_get_stats(wfe_ctx* ctx, wfe_stats* out)
         ctx->event_pool.push_back(t.stop);
     }
     ctx->timed.clear();
-    unsigned long long dev[2 * kNumTiers] = {};
+    unsigned long long dev[2 * kNumTiers + kMaxBuckets] = {};
     WFE_CUDA(ctx, cudaMemcpy(dev, ctx->d_passed, sizeof(dev), cudaMemcpyDeviceToHost));
     *out = ctx->stats;
     for (int t = 0; t < kNumTiers; ++t) {
         out->tier_passed[t] = dev[t];
-        if (t > ctx->first_tier) out->tier_entered[t] = dev[t - 1];
+        out->tier_entered[t] = ctx->single_entered[t] + (t > 0 ? dev[t - 1] : 0);
         out->tier_launches[t] += dev[kNumTiers + t];
         out->kernel_launches += dev[kNumTiers + t];
     }
+    for (int b = 0; b < ctx->nbuckets; ++b) out->tier_entered[ctx->bucket[b].first_tier] += dev[2 * kNumTiers + b];
     return WFE_OK;
 }
 
@@ -340,7 +519,8 @@ int wfe_reset_stats(wfe_ctx* ctx)
     const int r = wfe_get_stats(ctx, &tmp); /* drains pending timings */
     if (r != WFE_OK) return r;
     ctx->stats = wfe_stats{};
-    WFE_CUDA(ctx, cudaMemset(ctx->d_passed, 0, sizeof(unsigned long long) * 2 * kNumTiers));
+    for (auto& x : ctx->single_entered) x = 0;
+    WFE_CUDA(ctx, cudaMemset(ctx->d_passed, 0, sizeof(unsigned long long) * (2 * kNumTiers + kMaxBuckets)));
     return WFE_OK;
 }
 
@@ -352,6 +532,8 @@ int wfe_align_device(wfe_ctx* ctx, const char* d_ascii, const wfe_pair* d_pairs,
         return WFE_ERR_INVALID_ARGUMENT;
     if (max_len > ctx->cfg.max_seq_len) return WFE_ERR_SEQ_TOO_LONG;
     WFE_CUDA(ctx, cudaSetDevice(ctx->cfg.device));
+    /* an earlier asynchronous call whose device-side launch failed */
+    if (const int r = take_launch_error(ctx)) return r;
     cudaStream_t s = stream ? (cudaStream_t)stream : ctx->st[0].stream;
     const size_t B = ctx->cfg.batch_size;
     for (size_t b0 = 0; b0 < n; b0 += B) {
@@ -530,7 +712,7 @@ int align_host(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, in
         ctx->stats.pairs += nb;
     }
     for (int i = 0; i < nstages; ++i) WFE_CUDA(ctx, cudaStreamSynchronize(ctx->st[i].stream));
-    return WFE_OK;
+    return take_launch_error(ctx);
 }
 
 }  // namespace
@@ -632,3 +814,168 @@ void wfe_host_free(void* p)
 }
 
 }  // extern "C"
+
+/* ---- autotuner ------------------------------------------------------------ */
+
+namespace {
+
+/* One cache line per tuned context, JSON:
+ * {"gpu": "...", "max_seq_len": L, "cigar_stride": S, "buckets": [...], "first_tier": [...]} */
+std::string cache_key(const wfe_ctx* ctx, const char* gpu, uint32_t nb, const uint32_t* bmax, uint32_t flags)
+{
+    std::ostringstream k;
+    k << "{\"gpu\": \"" << gpu << "\", \"max_seq_len\": " << ctx->cfg.max_seq_len
+      << ", \"cigar_stride\": " << ctx->cfg.cigar_stride << ", \"flags\": " << flags << ", \"buckets\": [";
+    for (uint32_t b = 0; b < nb; ++b) k << (b ? ", " : "") << (b + 1 == nb ? ctx->cfg.max_seq_len : bmax[b]);
+    k << "], \"first_tier\": [";
+    return k.str();
+}
+
+bool cache_lookup(const char* path, const std::string& key, uint32_t nb, int32_t* tiers)
+{
+    if (!path) return false;
+    std::ifstream f(path);
+    std::string line;
+    bool found = false;
+    while (std::getline(f, line)) {
+        if (line.compare(0, key.size(), key) != 0) continue;
+        std::istringstream in(line.substr(key.size()));
+        uint32_t b = 0;
+        for (; b < nb; ++b) {
+            int v = -1;
+            char sep = 0;
+            if (!(in >> v)) break;
+            tiers[b] = v;
+            in >> sep;
+        }
+        found = (b == nb); /* the last matching line wins */
+    }
+    return found;
+}
+
+void cache_store(const char* path, const std::string& key, uint32_t nb, const int32_t* tiers)
+{
+    if (!path) return;
+    std::ofstream f(path, std::ios::app);
+    f << key;
+    for (uint32_t b = 0; b < nb; ++b) f << (b ? ", " : "") << tiers[b];
+    f << "]}\n";
+}
+
+}  // namespace
+
+extern "C" int wfe_autotune(wfe_ctx* ctx, const char* d_ascii, const wfe_pair* d_pairs, size_t n,
+                            uint32_t nbuckets, const uint32_t* bucket_max_len, uint32_t flags,
+                            const char* cache_path, int32_t* first_tier_out)
+{
+    if (!ctx || !d_ascii || !d_pairs || n == 0 || nbuckets < 1 || nbuckets > (uint32_t)kMaxBuckets ||
+        !bucket_max_len)
+        return WFE_ERR_INVALID_ARGUMENT;
+    const wfe_config& c = ctx->cfg;
+    WFE_CUDA(ctx, cudaSetDevice(c.device));
+    cudaDeviceProp prop{};
+    WFE_CUDA(ctx, cudaGetDeviceProperties(&prop, c.device));
+    const std::string key = cache_key(ctx, prop.name, nbuckets, bucket_max_len, flags);
+    int32_t best[kMaxBuckets];
+    if (cache_lookup(cache_path, key, nbuckets, best)) {
+        const int r = wfe_set_policy(ctx, nbuckets, bucket_max_len, best, flags);
+        if (r == WFE_OK && first_tier_out)
+            for (uint32_t b = 0; b < nbuckets; ++b) first_tier_out[b] = best[b];
+        if (r == WFE_OK) return WFE_OK; /* a stale entry falls through to tuning */
+    }
+    /* start from the length defaults, then time every usable first tier of
+     * every bucket on up to kSample of the given pairs that fall in it, run
+     * through the same routing and chains as a real batch */
+    int r = wfe_set_policy(ctx, nbuckets, bucket_max_len, nullptr, flags);
+    if (r != WFE_OK) return r;
+    constexpr size_t kSample = 4096;
+    const size_t ns = std::min<size_t>(n, std::max<size_t>(kSample * nbuckets, 65536));
+    std::vector<wfe_pair> host(ns);
+    WFE_CUDA(ctx, cudaMemcpy(host.data(), d_pairs, ns * sizeof(wfe_pair), cudaMemcpyDeviceToHost));
+    std::vector<std::vector<wfe_pair>> sample(nbuckets);
+    for (size_t i = 0; i < ns; ++i) {
+        const uint32_t len = std::max(host[i].p_len, host[i].t_len);
+        if (len > c.max_seq_len) continue;
+        uint32_t b = 0;
+        while (b + 1 < nbuckets && len > ctx->bucket[b].max_len) ++b;
+        if (sample[b].size() < std::min<size_t>(kSample, c.batch_size)) sample[b].push_back(host[i]);
+    }
+    wfe_pair* d_sample = nullptr;
+    int32_t* d_dist = nullptr;
+    int8_t* d_cigar = nullptr;
+    uint8_t* d_status = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    Stage& st = ctx->st[0];
+    cudaStream_t s = st.stream;
+    auto cleanup = [&]() {
+        cudaFree(d_sample); cudaFree(d_dist); cudaFree(d_cigar); cudaFree(d_status);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    };
+    cudaError_t e = cudaSuccess;
+    if ((e = cudaMalloc(&d_sample, kSample * sizeof(wfe_pair))) != cudaSuccess ||
+        (e = cudaMalloc(&d_dist, kSample * sizeof(int32_t))) != cudaSuccess ||
+        (e = cudaMalloc(&d_cigar, kSample * (size_t)c.cigar_stride + 16)) != cudaSuccess ||
+        (e = cudaMalloc(&d_status, kSample)) != cudaSuccess || (e = cudaEventCreate(&e0)) != cudaSuccess ||
+        (e = cudaEventCreate(&e1)) != cudaSuccess) {
+        cleanup();
+        return fail_cuda(ctx, e);
+    }
+    /* tuning runs do not count in the statistics */
+    const wfe_stats saved = ctx->stats;
+    uint64_t saved_entered[kNumTiers];
+    std::copy(ctx->single_entered, ctx->single_entered + kNumTiers, saved_entered);
+    unsigned long long saved_dev[2 * kNumTiers + kMaxBuckets];
+    if ((e = cudaMemcpy(saved_dev, ctx->d_passed, sizeof saved_dev, cudaMemcpyDeviceToHost)) != cudaSuccess) {
+        cleanup();
+        return fail_cuda(ctx, e);
+    }
+    int tiers[kMaxBuckets];
+    for (uint32_t b = 0; b < nbuckets; ++b) best[b] = tiers[b] = ctx->bucket[b].first_tier;
+    for (uint32_t b = 0; b < nbuckets; ++b) {
+        if (sample[b].empty()) continue;
+        const uint32_t m = (uint32_t)sample[b].size();
+        e = cudaMemcpy(d_sample, sample[b].data(), m * sizeof(wfe_pair), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) { cleanup(); return fail_cuda(ctx, e); }
+        Layout L{};
+        L.ascii = d_ascii;
+        L.pairs = d_sample;
+        const BucketPlan& bp = ctx->bucket[b];
+        float best_ms = 1e30f;
+        for (int t = 0; t <= bp.last_tier; ++t) {
+            BucketPlan trial = bp;
+            trial.first_tier = t;
+            if (!bucket_usable(trial)) continue;
+            tiers[b] = t;
+            float ms_min = 1e30f;
+            for (int rep = 0; rep < 3; ++rep) {
+                cudaEventRecord(e0, s);
+                r = run_chain(ctx, st, L, m, d_dist, d_cigar, d_status, s, tiers);
+                cudaEventRecord(e1, s);
+                if (r != WFE_OK || cudaEventSynchronize(e1) != cudaSuccess) { r = WFE_ERR_CUDA; break; }
+                if ((r = take_launch_error(ctx)) != WFE_OK) break;
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (rep > 0) ms_min = std::min(ms_min, ms); /* the first run warms up */
+            }
+            if (r != WFE_OK) { cleanup(); return r; }
+            if (ms_min < best_ms) {
+                best_ms = ms_min;
+                best[b] = t;
+            }
+        }
+        tiers[b] = best[b];
+    }
+    cleanup();
+    ctx->stats = saved;
+    std::copy(saved_entered, saved_entered + kNumTiers, ctx->single_entered);
+    WFE_CUDA(ctx, cudaMemcpy(ctx->d_passed, saved_dev, sizeof saved_dev, cudaMemcpyHostToDevice));
+    for (auto& t : ctx->timed) { ctx->event_pool.push_back(t.start); ctx->event_pool.push_back(t.stop); }
+    ctx->timed.clear();
+    r = wfe_set_policy(ctx, nbuckets, bucket_max_len, best, flags);
+    if (r != WFE_OK) return r;
+    cache_store(cache_path, key, nbuckets, best);
+    if (first_tier_out)
+        for (uint32_t b = 0; b < nbuckets; ++b) first_tier_out[b] = best[b];
+    return WFE_OK;
+}

@@ -25,10 +25,31 @@
 #include "wfe_kernels.cuh"
 
 #include <algorithm>
+#include <map>
+#include <mutex>
 
 namespace wfe {
 
 namespace {
+
+/* Raise, never lower, a kernel's dynamic shared memory limit on the current
+ * device.  The limit is a property of the kernel, and a tier launched on the
+ * device by one bucket's chain relies on it still covering that bucket after
+ * the host has launched the same tier for a smaller bucket. */
+cudaError_t allow_smem(const void* fn, size_t bytes)
+{
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, size_t> limit;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t& cur = limit[{fn, dev}];
+    if (bytes <= cur) return cudaSuccess;
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) cur = bytes;
+    return e;
+}
 
 constexpr int kWarps = 4;
 constexpr int kThreads = kWarps * 32;
@@ -112,7 +133,7 @@ size_t cta_smem_bytes(uint32_t max_len, uint32_t cigar_stride)
     return group_smem_bytes<T>(max_len, cigar_stride) * (size_t)(kWarps * T::GPW);
 }
 
-template <class T>
+template <class T, bool PREDICT = false>
 __global__ void __launch_bounds__(kThreads, T::MINB)
 tier_kernel(AlignLaunch A, uint32_t seq_words, uint32_t gbytes);
 
@@ -140,42 +161,67 @@ __device__ void launch_on_device(const AlignLaunch& a, uint32_t count)
     const uint32_t per_cta = (uint32_t)(kWarps * T::GPW);
     const int grid = max(1, min(sh.grid, (int)((count + per_cta - 1u) / per_cta)));
     tier_kernel<T><<<grid, kThreads, sh.smem, cudaStreamTailLaunch>>>(a, sh.seq_words, sh.gbytes);
-    if (a.chain.launched) atomicAdd(a.chain.launched + a.tier, 1ull);
 }
 
-/* Called by the last CTA of tier A.tier when it handed `count` pairs on:
- * the next tier runs over them once this grid has completed. */
-__device__ __noinline__ void launch_next_tier(const AlignLaunch& A, uint32_t count)
+/* Called by the last CTA of tier A.tier: tier u (> A.tier) runs over its
+ * list of `count` pairs once this grid has completed. */
+__device__ __noinline__ void launch_tier_on_device(const AlignLaunch& A, int u, uint32_t count)
 {
     AlignLaunch n = A;
-    n.tier = A.tier + 1;
-    n.work = A.retry;
-    n.work_count = A.retry_count;
-    n.retry = n.tier < A.chain.last_tier ? (A.retry == A.chain.lists[0] ? A.chain.lists[1] : A.chain.lists[0])
-                                         : nullptr;
-    n.retry_count = A.chain.counts + n.tier;
-    n.passed_total = A.passed_total ? A.passed_total + 1 : nullptr;
-    switch (n.tier) {
+    n.tier = u;
+    n.work = A.chain.list[u];
+    n.work_count = A.chain.counts + u;
+    n.retry = u < A.chain.last_tier ? A.chain.list[u + 1] : nullptr;
+    n.retry_count = A.chain.counts + u + 1;
+    n.passed_total = A.chain.passed ? A.chain.passed + u : nullptr;
+    switch (u) {
     case 1: launch_on_device<T1>(n, count); break;
     case 2: launch_on_device<T2>(n, count); break;
     case 3: launch_on_device<T3>(n, count); break;
     case 4: launch_on_device<T4>(n, count); break;
     case 5:
     case 6: {
-        const TierShape& sh = n.chain.shape[n.tier];
+        const TierShape& sh = n.chain.shape[u];
         const int grid = max(1, min(sh.grid, (int)count));
-        if (n.tier == 5)
+        if (u == 5)
             long_kernel<false><<<grid, kLongThreads, sh.smem, cudaStreamTailLaunch>>>(n);
         else
             long_kernel<true><<<grid, kLongThreads, sh.smem, cudaStreamTailLaunch>>>(n);
-        if (n.chain.launched) atomicAdd(n.chain.launched + n.tier, 1ull);
         break;
     }
-    default: break;
+    default: return;
+    }
+    if (cudaGetLastError() != cudaSuccess) {
+        /* the pairs of tier u and above stay unaligned: tell the host */
+        if (n.chain.launch_error) atomicOr_system(n.chain.launch_error, 1u << u);
+        return;
+    }
+    if (n.chain.launched) atomicAdd(n.chain.launched + u, 1ull);
+}
+
+/* End of a tier kernel: the last CTA to finish starts the next tier that has
+ * work (pairs handed on by this tier, or routed to it up front). */
+__device__ __forceinline__ void chain_next(const AlignLaunch& A)
+{
+    if (!A.chain.cta_done) return;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned t = atomicAdd(A.chain.cta_done + A.tier, 1u);
+        if (t == gridDim.x - 1u) {
+            __threadfence();
+            for (int u = A.tier + 1; u <= A.chain.last_tier; ++u) {
+                const uint32_t cnt = *reinterpret_cast<volatile const uint32_t*>(A.chain.counts + u);
+                if (cnt > 0u) {
+                    launch_tier_on_device(A, u, cnt);
+                    break;
+                }
+            }
+        }
     }
 }
 
-template <class T>
+template <class T, bool PREDICT>
 __global__ void __launch_bounds__(kThreads, T::MINB)
 tier_kernel(AlignLaunch A, uint32_t seq_words, uint32_t gbytes)
 {
@@ -206,8 +252,17 @@ tier_kernel(AlignLaunch A, uint32_t seq_words, uint32_t gbytes)
     int* runs = reinterpret_cast<int*>(uni + round16(A.cigar_stride));
 
     const uint32_t count = A.work_count ? min(*A.work_count, A.n_work) : A.n_work;
+    /* work stealing: each warp takes the next GPW items from the launch's
+     * counter (or, without one, every gridDim-th block of items) */
+    uint32_t* const work_next = A.chain.work_next ? A.chain.work_next + A.tier : nullptr;
     const uint32_t step = gridDim.x * (uint32_t)(kWarps * GPW);
-    for (uint32_t wb = (blockIdx.x * kWarps + (uint32_t)warp) * GPW; wb < count; wb += step) {
+    uint32_t wb = (blockIdx.x * kWarps + (uint32_t)warp) * GPW;
+    if (work_next) {
+        uint32_t v = 0;
+        if (lane == 0) v = atomicAdd(work_next, (uint32_t)GPW);
+        wb = __shfl_sync(kFull, v, 0);
+    }
+    for (; wb < count;) {
         const uint32_t item = wb + (uint32_t)grp;
         int state = ST_IDLE;
         uint32_t pi = 0;
@@ -218,10 +273,12 @@ tier_kernel(AlignLaunch A, uint32_t seq_words, uint32_t gbytes)
             pr = get_pair(A.L, pi);
             const uint32_t mx = max(pr.plen, pr.tlen);
             state = !pr.in_range ? ST_RANGE
+                    : PREDICT ? ST_RUN
                     : (mx > A.max_len || mx > 16u * seq_words) ? ST_TOOLONG : ST_RUN;
         }
-        const uint32_t lp = state == ST_RUN ? pr.plen : 0u;
-        const uint32_t lt = state == ST_RUN ? pr.tlen : 0u;
+        /* a prediction launch aligns only the first kPredictPrefix bases */
+        const uint32_t lp = state == ST_RUN ? (PREDICT ? min(pr.plen, (uint32_t)kPredictPrefix) : pr.plen) : 0u;
+        const uint32_t lt = state == ST_RUN ? (PREDICT ? min(pr.tlen, (uint32_t)kPredictPrefix) : pr.tlen) : 0u;
         load_packed<G, T::RMAX>(pr.p, lp, QP, g, gmask);
         load_packed<G, T::RMAX>(pr.t, lt, QT, g, gmask);
         __syncwarp();
@@ -263,7 +320,7 @@ tier_kernel(AlignLaunch A, uint32_t seq_words, uint32_t gbytes)
                     const int m = max(max(del_p, sub_p), ins_p);
                     const unsigned blo = __ballot_sync(kFull, m & 1);
                     const unsigned bhi = __ballot_sync(kFull, m & 2);
-                    if (run && g == 0)
+                    if (!PREDICT && run && g == 0)
                         OE::put(ops, rowbase + c, (blo >> ((grp * G) & 31)) & gbits,
                                 (bhi >> ((grp * G) & 31)) & gbits);
                     const int k = lo_k + g;
@@ -290,6 +347,11 @@ tier_kernel(AlignLaunch A, uint32_t seq_words, uint32_t gbytes)
             }
         }
 
+        if constexpr (PREDICT) {
+            if (g == 0 && item < count)
+                A.pred[pi] = (uint16_t)(state == ST_DONE ? D : (state == ST_OVERFLOW ? DCAP + 1 : 0xffff));
+            state = ST_IDLE;
+        }
         if (state == ST_DONE) {
             /* backtrace: from (D, kt) back to (0, 0); a walk that leaves the
              * wavefront (never expected) is reported, not followed */
@@ -341,21 +403,17 @@ tier_kernel(AlignLaunch A, uint32_t seq_words, uint32_t gbytes)
             }
         }
         __syncwarp();
-    }
-
-    /* the last CTA to finish starts the next tier if this one handed pairs on */
-    if (A.chain.cta_done) {
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            __threadfence();
-            const unsigned t = atomicAdd(A.chain.cta_done + A.tier, 1u);
-            if (t == gridDim.x - 1u) {
-                __threadfence();
-                const uint32_t cnt = *reinterpret_cast<volatile const uint32_t*>(A.retry_count);
-                if (cnt > 0u && A.tier < A.chain.last_tier) launch_next_tier(A, cnt);
-            }
+        if (work_next) {
+            uint32_t v = 0;
+            if (lane == 0) v = atomicAdd(work_next, (uint32_t)GPW);
+            wb = __shfl_sync(kFull, v, 0);
+        } else {
+            wb += step;
         }
     }
+
+    /* the last CTA to finish starts the next tier that has work */
+    if constexpr (!PREDICT) chain_next(A);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -405,7 +463,15 @@ __global__ void __launch_bounds__(kLongThreads) long_kernel(AlignLaunch A)
     int* bufB = wf + W + dlim + 2;
 
     const uint32_t count = A.work_count ? min(*A.work_count, A.n_work) : A.n_work;
-    for (uint32_t item = blockIdx.x; item < count; item += gridDim.x) {
+    __shared__ uint32_t s_item;
+    uint32_t* const work_next = A.chain.work_next ? A.chain.work_next + A.tier : nullptr;
+    uint32_t item = blockIdx.x;
+    if (work_next) {
+        if (threadIdx.x == 0) s_item = atomicAdd(work_next, 1u);
+        __syncthreads();
+        item = s_item;
+    }
+    while (item < count) {
         const uint32_t pi = A.work ? A.work[item] : item;
         const PairRef pr = get_pair(A.L, pi);
         const uint32_t mx = max(pr.plen, pr.tlen);
@@ -521,20 +587,16 @@ __global__ void __launch_bounds__(kLongThreads) long_kernel(AlignLaunch A)
             }
         }
         __syncthreads();
-    }
-
-    if (A.chain.cta_done) {
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            __threadfence();
-            const unsigned t = atomicAdd(A.chain.cta_done + A.tier, 1u);
-            if (t == gridDim.x - 1u) {
-                __threadfence();
-                const uint32_t cnt = *reinterpret_cast<volatile const uint32_t*>(A.retry_count);
-                if (cnt > 0u && A.tier < A.chain.last_tier) launch_next_tier(A, cnt);
-            }
+        if (work_next) {
+            if (threadIdx.x == 0) s_item = atomicAdd(work_next, 1u);
+            __syncthreads();
+            item = s_item;
+        } else {
+            item += gridDim.x;
         }
     }
+
+    chain_next(A);
 }
 
 const TierInfo kTiers[kNumTiers] = {
@@ -553,7 +615,7 @@ TierShape shape_of(uint32_t max_len, uint32_t cigar_stride, int sm_count)
     TierShape sh{};
     const size_t smem = cta_smem_bytes<T>(max_len, cigar_stride);
     if (smem > 227u * 1024u) return sh;
-    if (cudaFuncSetAttribute(tier_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    if (allow_smem((const void*)tier_kernel<T>, smem) != cudaSuccess)
         return sh;
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, tier_kernel<T>, kThreads, smem) != cudaSuccess)
@@ -580,11 +642,62 @@ cudaError_t launch(const AlignLaunch& a, int grid, cudaStream_t s)
     if (smem > 227u * 1024u) return cudaErrorInvalidValue;
     if (!T::SMEM_OPS && a.ops_scratch_bytes < T::ops_bytes * (size_t)grid * (kWarps * T::GPW))
         return cudaErrorInvalidValue;
-    cudaError_t e = cudaFuncSetAttribute(tier_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    cudaError_t e = allow_smem((const void*)tier_kernel<T>, smem);
     if (e != cudaSuccess) return e;
     tier_kernel<T><<<grid, kThreads, smem, s>>>(a, sw, (uint32_t)gb);
     return cudaGetLastError();
+}
+
+/* ------------------------------------------------------------------------ */
+/* Routing: one thread per pair.  The length bucket is the first whose
+ * max_len holds max(p_len, t_len).  The tier is the bucket's first tier, or,
+ * with predictions, the first tier whose distance limit covers the
+ * prediction: the prefix distance scaled by max length / prefix length,
+ * plus 25 % and 2, up to tier 5 (a prediction only chooses where a pair
+ * starts; a pair above its tier's limit still moves up).  Appends are warp-aggregated: one
+ * atomic per (bucket, tier) present in the warp. */
+__global__ void __launch_bounds__(256) classify_kernel(Layout L, uint32_t n, Buckets B)
+{
+    const int lane = (int)(threadIdx.x & 31u);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t lim = (n + 31u) & ~31u; /* whole warps iterate together */
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < lim; i += stride) {
+        int key = -1;
+        if (i < n) {
+            const PairRef pr = get_pair(L, i);
+            const uint32_t len = max(pr.plen, pr.tlen);
+            int b = B.n - 1;
+            for (int j = 0; j < B.n; ++j)
+                if (len <= B.max_len[j]) { b = j; break; }
+            int t = B.first_tier[b];
+            if (B.pred && len > 0) {
+                const uint32_t pref = min(max(pr.plen, pr.tlen), (uint32_t)kPredictPrefix);
+                const uint32_t pd = B.pred[i];
+                if (pd != 0xffff) {
+                    const float scale = (float)len / (float)max(pref, 1u);
+                    const float est = ((float)pd + 1.0f) * scale * 1.25f + 2.0f;
+                    /* never past tier 5: the global-wavefront tier only
+                     * takes pairs that tier 5 hands on */
+                    const int top = min(B.last_tier[b], 5);
+                    while (t < top && (float)B.dcap[t] < est) ++t;
+                }
+            }
+            key = b * kNumTiers + t;
+        }
+        const unsigned same = __match_any_sync(kFull, key);
+        const int leader = __ffs((int)same) - 1;
+        uint32_t base = 0;
+        if (key >= 0 && lane == leader) {
+            const int b = key / kNumTiers, t = key % kNumTiers;
+            base = atomicAdd(B.counts + (size_t)b * B.count_stride + t, (uint32_t)__popc(same));
+            if (B.totals) atomicAdd(B.totals + b, (unsigned long long)__popc(same));
+        }
+        base = __shfl_sync(kFull, base, leader);
+        if (key >= 0) {
+            const uint32_t rank = (uint32_t)__popc(same & ((1u << lane) - 1u));
+            B.lists[(size_t)key * B.stride + base + rank] = i;
+        }
+    }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -696,7 +809,7 @@ TierShape long_shape_of(uint32_t max_len, int sm_count)
     const uint32_t sw = seq_words_for(max_len);
     const size_t smem = 16u * (size_t)sw + (GWF ? 0u : 8u * (size_t)(2 * dlim + 5));
     if (smem > 227u * 1024u) return sh;
-    if (cudaFuncSetAttribute(long_kernel<GWF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    if (allow_smem((const void*)long_kernel<GWF>, smem) != cudaSuccess)
         return sh;
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, long_kernel<GWF>, kLongThreads, smem) != cudaSuccess)
@@ -714,7 +827,7 @@ cudaError_t launch_long(const AlignLaunch& a, int grid, cudaStream_t s)
 {
     const TierShape& sh = a.chain.shape[a.tier];
     if (!sh.scratch || sh.smem == 0) return cudaErrorInvalidValue;
-    cudaError_t e = cudaFuncSetAttribute(long_kernel<GWF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem);
+    cudaError_t e = allow_smem((const void*)long_kernel<GWF>, sh.smem);
     if (e != cudaSuccess) return e;
     long_kernel<GWF><<<grid, kLongThreads, sh.smem, s>>>(a);
     return cudaGetLastError();
@@ -756,6 +869,34 @@ cudaError_t launch_tier(int tier, const AlignLaunch& a, int grid, cudaStream_t s
     }
 }
 
+cudaError_t launch_classify(const Layout& L, uint32_t n, const Buckets& B, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    const uint32_t blocks = std::min<uint32_t>((n + 255u) / 256u, 4096u);
+    classify_kernel<<<blocks, 256, 0, s>>>(L, n, B);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_predict(const Layout& L, uint32_t n, uint32_t max_len, uint16_t* pred, int grid, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    const uint32_t plen = std::min<uint32_t>(max_len, (uint32_t)kPredictPrefix);
+    const size_t gb = group_smem_bytes<T0>(plen, 0);
+    const size_t smem = gb * (size_t)(kWarps * T0::GPW);
+    cudaError_t e = allow_smem((const void*)tier_kernel<T0, true>, smem);
+    if (e != cudaSuccess) return e;
+    AlignLaunch a{};
+    a.L = L;
+    a.n_work = n;
+    a.max_len = max_len;
+    a.pred = pred;
+    a.tier = 0;
+    const uint32_t per_cta = kWarps * T0::GPW;
+    grid = std::max(1, std::min(grid, (int)((n + per_cta - 1) / per_cta)));
+    tier_kernel<T0, true><<<grid, kThreads, smem, s>>>(a, seq_words_for(plen), (uint32_t)gb);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_pack(const Layout& L, uint32_t n, uint32_t* words, uint32_t wps, cudaStream_t s)
 {
     if (n == 0) return cudaSuccess;
@@ -774,8 +915,7 @@ cudaError_t launch_cigar_from_history(const Layout& L, uint32_t n, uint32_t max_
     const size_t gb = 16u * (size_t)sw + 64u + 256u + round16(stride);
     const size_t smem = gb * (size_t)(kWarps * (32 / kHG));
     if (smem > 227u * 1024u) return cudaErrorInvalidValue;
-    cudaError_t e = cudaFuncSetAttribute(history_cigar_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    cudaError_t e = allow_smem((const void*)history_cigar_kernel, smem);
     if (e != cudaSuccess) return e;
     const uint32_t per_cta = kWarps * (32 / kHG);
     const uint32_t blocks = std::min<uint32_t>((n + per_cta - 1u) / per_cta, 1u << 20);

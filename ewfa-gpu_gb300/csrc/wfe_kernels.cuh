@@ -42,16 +42,39 @@ struct TierShape {
  * operation chain, runs, and for tier 6 the two wavefront buffers. */
 uint64_t long_slab_bytes(int dlim, bool global_wavefront);
 
-/* The tier chain of one batch.  Each tier kernel's last CTA launches the
- * next tier as a tail launch when it handed any pair on, so no launch is
- * made for a tier that has no work. */
+/* The tier chain of one batch (of one length bucket).  Tier t works on the
+ * pairs of its list: those routed to it up front and those that tier t-1
+ * handed on.  Each tier kernel's last CTA launches, as a tail launch, the
+ * next tier whose list is not empty, so no launch is made for a tier that
+ * has no work. */
 struct Chain {
     int last_tier;                   /* last tier of the chain */
     TierShape shape[kNumTiers];
-    uint32_t* lists[2];              /* work lists, used alternately by the tiers */
-    uint32_t* counts;                /* counts[t]: pairs tier t handed on */
+    uint32_t* list[kNumTiers];       /* list[t]: work of tier t */
+    uint32_t* counts;                /* counts[t]: pairs in list[t] */
     uint32_t* cta_done;              /* cta_done[t]: CTAs of tier t that finished */
+    uint32_t* work_next;             /* work_next[t]: next work item of tier t (work stealing) */
     unsigned long long* launched;    /* launched[t]: launches of tier t (stats) */
+    unsigned long long* passed;      /* passed[t]: pairs tier t handed on (stats) */
+    uint32_t* launch_error;          /* bit t: a device-side launch of tier t failed (host-mapped) */
+};
+
+/* Length buckets of the classify kernel, and for each the tiers a pair may
+ * be routed to by its predicted distance. */
+constexpr int kMaxBuckets = 8;
+constexpr int kPredictPrefix = 128; /* bases of each sequence the distance prediction aligns */
+struct Buckets {
+    int n;
+    uint32_t max_len[kMaxBuckets];   /* ascending; a pair goes to the first bucket that holds it */
+    int first_tier[kMaxBuckets];
+    int last_tier[kMaxBuckets];
+    int dcap[kNumTiers];             /* largest distance of each tier */
+    const uint16_t* pred;            /* predicted prefix distances, or NULL (route to first_tier) */
+    uint32_t* lists;                 /* list of bucket b, tier t at lists + (b*kNumTiers + t)*stride */
+    uint32_t stride;
+    uint32_t* counts;                /* counts of bucket b at counts + b*count_stride */
+    uint32_t count_stride;
+    unsigned long long* totals;      /* pairs classified into each bucket (stats) */
 };
 
 /* Arguments of one alignment launch over a work list. */
@@ -70,6 +93,7 @@ struct AlignLaunch {
                                     NULL = last tier: they get WFE_PAIR_TOO_LONG */
     uint32_t* retry_count;
     unsigned long long* passed_total; /* running count of pairs handed on (stats) */
+    uint16_t* pred;              /* prediction launch: prefix distance of every pair */
     unsigned char* ops_scratch;  /* global op store for tiers that keep it there */
     size_t ops_scratch_bytes;
     int tier;                    /* this launch's tier */
@@ -86,6 +110,15 @@ size_t tier_scratch_bytes(int tier, int grid);
  * cigar_stride (occupancy-limited, at least 1). */
 int tier_grid(int tier, uint32_t max_len, uint32_t cigar_stride, int sm_count);
 cudaError_t launch_tier(int tier, const AlignLaunch& a, int grid, cudaStream_t s);
+
+/* Sort pairs 0..n-1 into length buckets by max(p_len, t_len) and, within a
+ * bucket, into the tier of their predicted distance (see Buckets). */
+cudaError_t launch_classify(const Layout& L, uint32_t n, const Buckets& B, cudaStream_t s);
+
+/* Distance of the first kPredictPrefix bases of every pair (capped at
+ * tier 0's limit + 1), for routing: pred[i] for pair i. */
+cudaError_t launch_predict(const Layout& L, uint32_t n, uint32_t max_len, uint16_t* pred, int grid,
+                           cudaStream_t s);
 
 cudaError_t launch_pack(const Layout& L, uint32_t n, uint32_t* words,
                         uint32_t words_per_seq, cudaStream_t s);

@@ -25,6 +25,7 @@ PAIR_OK, PAIR_OVER_MAX_DISTANCE, PAIR_CIGAR_TRUNCATED, PAIR_TOO_LONG, PAIR_BAD_H
 PAIR_OUT_OF_RANGE = 5
 FLAG_NO_PIPELINE = 1
 FLAG_KERNEL_TIMING = 2
+POLICY_PREDICT = 1
 
 PAIR_DTYPE = np.dtype([("p_off", "<u8"), ("t_off", "<u8"), ("p_len", "<u4"), ("t_len", "<u4")])
 assert PAIR_DTYPE.itemsize == 24
@@ -34,7 +35,7 @@ SYMBOLS = [
     "wfe_reset_stats", "wfe_align", "wfe_align_strided", "wfe_align_device", "wfe_pack_device",
     "wfe_cigar_from_history_device", "wfe_format_cigar", "wfe_check_cigar", "wfe_align_device_noalloc",
     "wfe_read_pair_file", "wfe_free_pair_file", "wfe_host_alloc", "wfe_host_free", "wfe_device_count",
-    "wfe_device_name",
+    "wfe_device_name", "wfe_set_policy", "wfe_get_policy", "wfe_autotune",
 ]
 NOALLOC_MAX_DISTANCE = 271
 NOALLOC_SCRATCH_BYTES = 16 << 20
@@ -102,6 +103,9 @@ def load() -> C.CDLL:
     L.wfe_format_cigar.restype = sz
     L.wfe_check_cigar.argtypes = [C.c_char_p, u32, C.c_char_p, u32, vp, sz, C.POINTER(i32)]
     L.wfe_align_device_noalloc.argtypes = [vp, vp, sz, u32, i32, vp, vp, u32, vp, vp]
+    L.wfe_set_policy.argtypes = [vp, u32, vp, vp, u32]
+    L.wfe_get_policy.argtypes = [vp, C.POINTER(C.c_uint32), vp, vp, C.POINTER(C.c_uint32)]
+    L.wfe_autotune.argtypes = [vp, vp, vp, sz, u32, vp, u32, C.c_char_p, vp]
     L.wfe_read_pair_file.argtypes = [C.c_char_p, sz, C.c_int, C.c_int, C.POINTER(PairFileC), C.c_char_p, sz]
     L.wfe_free_pair_file.argtypes = [C.POINTER(PairFileC)]
     L.wfe_free_pair_file.restype = None
@@ -278,6 +282,31 @@ class Context:
 
     def reset_stats(self) -> None:
         _check(load().wfe_reset_stats(self._h), "wfe_reset_stats")
+
+    def set_policy(self, bucket_max_len, first_tier=None, predict: bool = False) -> None:
+        """Length buckets (ascending max lengths), each bucket's first tier
+        (-1 = by length) and distance prediction; see wfe_set_policy."""
+        bm = np.ascontiguousarray(bucket_max_len, dtype=np.uint32)
+        ft = None if first_tier is None else np.ascontiguousarray(first_tier, dtype=np.int32)
+        _check(load().wfe_set_policy(self._h, len(bm), _addr(bm), _addr(ft), POLICY_PREDICT if predict else 0),
+               "wfe_set_policy")
+
+    def policy(self):
+        nb, fl = C.c_uint32(0), C.c_uint32(0)
+        bm = np.zeros(8, np.uint32)
+        ft = np.zeros(8, np.int32)
+        _check(load().wfe_get_policy(self._h, C.byref(nb), _addr(bm), _addr(ft), C.byref(fl)), "wfe_get_policy")
+        return bm[:nb.value].tolist(), ft[:nb.value].tolist(), bool(fl.value & POLICY_PREDICT)
+
+    def autotune(self, d_ascii, d_pairs, n: int, bucket_max_len, cache_path: str | None = None,
+                 predict: bool = False):
+        """Measure every bucket's best first tier on device-resident pairs; returns the tiers."""
+        bm = np.ascontiguousarray(bucket_max_len, dtype=np.uint32)
+        out = np.zeros(len(bm), np.int32)
+        _check(load().wfe_autotune(self._h, _addr(d_ascii), _addr(d_pairs), n, len(bm), _addr(bm),
+                                   POLICY_PREDICT if predict else 0,
+                                   cache_path.encode() if cache_path else None, _addr(out)), "wfe_autotune")
+        return out.tolist()
 
     def align(self, ascii: np.ndarray, pairs: np.ndarray, out=None):
         """Host buffers in, host buffers out: (dist int32[n], cigar int8[n, stride], status uint8[n])."""

@@ -135,6 +135,53 @@ int wfe_last_cuda_error(const wfe_ctx* ctx);
 int wfe_get_stats(wfe_ctx* ctx, wfe_stats* out);
 int wfe_reset_stats(wfe_ctx* ctx);
 
+/* ---- scheduling policy (mixed lengths) ------------------------------------ */
+
+#define WFE_MAX_BUCKETS 8
+
+/* Length buckets: a pair goes to the first bucket whose bucket_max_len is at
+ * least max(p_len, t_len) (the last bucket always ends at max_seq_len).
+ * With more than one bucket, every batch is first sorted into buckets on the
+ * device and each bucket is aligned with launch shapes sized to its longest
+ * sequence -- shared memory per pair, resident CTAs -- starting at its own
+ * first tier:
+ *   tier 0: 4 lanes per pair, backtrace store in shared memory, distance <= 21
+ *   tier 1: 32 lanes per pair, shared-memory store, <= 79
+ *   tier 2: 32 lanes, shared-memory store, <= 143
+ *   tier 3: 32 lanes, store spilled to global memory, <= 271
+ *   tier 4: 32 lanes, global store, <= 527
+ *   tier 5: a CTA per pair, wavefront in shared memory, <= 2047
+ *   tier 6: a CTA per pair, wavefront in global memory, no limit
+ * (a pair above its tier's limit is handed to the next tier on the device).
+ * first_tier[b] = -1 picks by length; first_tier may be NULL.  With
+ * WFE_POLICY_PREDICT, a first pass aligns the first 128 bases of every pair
+ * (distance only) and each pair starts at the lowest tier of its bucket, not
+ * below first_tier[b], whose limit covers its distance extrapolated to its
+ * length: pairs of one length but very different error rates no longer all
+ * start at the same tier (and restart in every tier they outgrow).  Results
+ * do not depend on the policy.  The default is one bucket, no prediction.
+ * Replaces nothing in the reference, which has one fixed launch shape
+ * (src/wavefront.cu:173-208); see also wfe_autotune. */
+#define WFE_POLICY_PREDICT 1u /* route every pair to the tier of its predicted distance */
+int wfe_set_policy(wfe_ctx* ctx, uint32_t nbuckets, const uint32_t* bucket_max_len,
+                   const int32_t* first_tier, uint32_t flags);
+int wfe_get_policy(const wfe_ctx* ctx, uint32_t* nbuckets, uint32_t* bucket_max_len,
+                   int32_t* first_tier, uint32_t* flags);
+
+/* Choose every bucket's first tier by measurement and install the policy:
+ * for each bucket, up to 4096 of the given DEVICE pairs that fall in it are
+ * aligned starting at every usable tier (the tier fixes the lanes per pair,
+ * whether the backtrace store stays in shared memory or spills to global
+ * memory, and whether the wavefront stays in shared memory), through the
+ * same routing as a real batch (flags as in wfe_set_policy), and the
+ * fastest wins.  With cache_path set, a matching earlier result (same GPU,
+ * max_seq_len, slot size, flags and buckets) is reused instead, and new
+ * results are appended to that file.  first_tier_out (may be NULL) receives
+ * the choice. */
+int wfe_autotune(wfe_ctx* ctx, const char* d_ascii, const wfe_pair* d_pairs, size_t n,
+                 uint32_t nbuckets, const uint32_t* bucket_max_len, uint32_t flags,
+                 const char* cache_path, int32_t* first_tier_out);
+
 /* ---- host-buffer alignment (the reference's batch loop) --------------- */
 
 /* Align n pairs held in HOST memory; results to HOST memory.  Replaces the
@@ -174,9 +221,11 @@ int wfe_align_strided(wfe_ctx* ctx, const char* ascii, size_t stride,
  * context's stream), asynchronous.  max_len: an upper bound on every p_len
  * and t_len of the call (pairs above it get WFE_PAIR_TOO_LONG).  The ASCII
  * buffer must stay readable up to the next 16-byte boundary after every
- * sequence (sequences are read in aligned 16-byte blocks).  Replaces the
- * kernel chain WF_edit_distance -> generate_cigars
- * (src/wavefront.cu:203-260). */
+ * sequence (sequences are read in aligned 16-byte blocks).  A tier that a
+ * kernel failed to launch on the device (its pairs are left unaligned) is
+ * reported as WFE_ERR_CUDA by the next call on the context; wfe_align and
+ * wfe_align_strided report it themselves.  Replaces the kernel chain
+ * WF_edit_distance -> generate_cigars (src/wavefront.cu:203-260). */
 int wfe_align_device(wfe_ctx* ctx, const char* d_ascii,
                      const wfe_pair* d_pairs, size_t n, uint32_t max_len,
                      int32_t* d_dist, int8_t* d_cigar, uint8_t* d_status,

@@ -387,3 +387,50 @@ def test_long_tiers_without_distance_limit():
     assert stats["tier_passed"][4] > 0 and stats["tier_passed"][5] > 0, stats
     assert (st == 0).all()
     compare_with_oracle(ascii, pairs, 12000, dist, cg, st)
+
+
+def test_length_buckets_same_results():
+    """Mixed lengths sorted into length buckets, each with its own first tier
+    and launch shapes: every result equals the oracle's and the one-bucket
+    path's."""
+    torch_cuda()
+    ascii, pairs = wfe.generate(6000, 100, 3000, p_min=0.01, p_max=0.15, seed=17)
+    with wfe.Context(max_seq_len=3200, cigar_stride=2048, batch_size=2500) as ctx:
+        one = ctx.align(ascii, pairs)
+        for predict in (False, True):
+            # [2, 2, 1, 1, 1]: the host launches tier 2 for short buckets after
+            # longer buckets' chains have queued device-side tier-2 launches
+            for tiers in ([0, 0, 1, 2, 3], [-1, -1, -1, -1, -1], [0, 1, 2, 3, 5], [5, 5, 5, 5, 5],
+                          [2, 2, 1, 1, 1], [1, 2, 1, 2, 1]):
+                ctx.set_policy([256, 512, 1024, 2048, 3200], tiers, predict=predict)
+                got = ctx.align(ascii, pairs)
+                np.testing.assert_array_equal(got[0], one[0])
+                np.testing.assert_array_equal(got[2], one[2])
+                assert_same_cigars(got[1], one[1])
+            assert ctx.policy()[0] == [256, 512, 1024, 2048, 3200]
+            assert ctx.policy()[2] == predict
+    compare_with_oracle(ascii, pairs, 2048, *one)
+
+
+def test_autotune_installs_and_caches(tmp_path):
+    torch = torch_cuda()
+    ascii, pairs = wfe.generate(8000, 100, 3000, p_min=0.01, p_max=0.15, seed=18)
+    d_ascii = torch.from_numpy(ascii).cuda()
+    d_pairs = torch.from_numpy(pairs.view(np.uint8)).cuda()
+    cache = str(tmp_path / "tune.jsonl")
+    buckets = [256, 512, 1024, 2048, 3200]
+    with wfe.Context(max_seq_len=3200, cigar_stride=2048) as ctx:
+        tiers = ctx.autotune(d_ascii, d_pairs, len(pairs), buckets, cache, predict=True)
+        assert len(tiers) == 5 and all(0 <= t <= 6 for t in tiers)
+        assert ctx.policy() == (buckets, tiers, True)
+        assert ctx.stats()["pairs"] == 0  # tuning runs are not counted
+        got = ctx.align(ascii, pairs)
+    assert open(cache).read().count("first_tier") == 1
+    with wfe.Context(max_seq_len=3200, cigar_stride=2048) as ctx2:
+        assert ctx2.autotune(d_ascii, d_pairs, len(pairs), buckets, cache, predict=True) == tiers  # from the cache
+    assert open(cache).read().count("first_tier") == 1
+    with wfe.Context(max_seq_len=3200, cigar_stride=2048) as ctx3:
+        ctx3.autotune(d_ascii, d_pairs, len(pairs), buckets, cache)  # other flags: a new entry
+        assert ctx3.policy()[2] is False
+    assert open(cache).read().count("first_tier") == 2
+    compare_with_oracle(ascii, pairs, 2048, *got)
