@@ -57,9 +57,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["short", "mixed"], default="short",
+    ap.add_argument("--workload", choices=["short", "mixed", "serve"], default="short",
                     help="short: the short-read throughput workload (the metric's configuration); "
-                         "mixed: uneven lengths, plain fixed-shape launches vs length buckets")
+                         "mixed: uneven lengths, plain fixed-shape launches vs length buckets; "
+                         "serve: Poisson request stream, the request server vs one call per request")
+    ap.add_argument("--requests", type=int, default=0, help="serve workload: number of requests (default 1,000)")
     ap.add_argument("--pairs", type=int, default=0, help="mixed workload: number of pairs (default 2,000,000)")
     ap.add_argument("--profile-batch", type=int, default=0,
                     help="profiling case: align this many pairs of the workload as ONE batch, twice "
@@ -162,6 +164,141 @@ def run_mixed(args) -> int:
             "distance": {"mean": float(dist.mean()), "max": int(dist.max())}}
     print(json.dumps(line))
     return 0 if same_dist and same_status and ok_status else 1
+
+
+SERVE_REQUESTS, SERVE_MAX_PAIRS, SERVE_LMIN, SERVE_LMAX, SERVE_PMIN, SERVE_PMAX, SERVE_SEED = \
+    1000, 4096, 100, 5000, 0.01, 0.10, 7
+SERVE_BUCKETS = [256, 512, 1024, 2048, SERVE_LMAX]
+SERVE_RATES = [0.1, 0.25, 0.5, 0.75, 0.9, 1.0, 1.2]
+
+
+def run_serve(args) -> int:
+    """Served stream: requests of 1-4,096 pairs (log-uniform), lengths
+    log-uniform in [100, 5,000], edit probability uniform in [0.01, 0.10],
+    arriving as a Poisson stream at 10 %-120 % of the server's measured peak
+    throughput.  For each rate the same arrivals go (1) to the request
+    server (continuous batching over 4 streams, device-memory admission) and
+    (2) to the plain form, one blocking wfe_align call per request in
+    arrival order.  Latency = completion - scheduled arrival.  Both forms use
+    the same length buckets and first tiers (chosen by the autotuner on a
+    sample) and must give identical results."""
+    import threading
+    import torch
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(SERVE_SEED)
+    nreq = args.requests or SERVE_REQUESTS
+    sizes = np.floor(np.exp(rng.uniform(0, np.log(SERVE_MAX_PAIRS + 1), nreq))).astype(np.int64)
+    sizes = sizes.clip(1, SERVE_MAX_PAIRS)
+    starts = np.concatenate([[0], np.cumsum(sizes)[:-1]])
+    total = int(sizes.sum())
+    ascii, pairs = wfe.generate(total, SERVE_LMIN, SERVE_LMAX, p_min=SERVE_PMIN, p_max=SERVE_PMAX, seed=SERVE_SEED)
+    max_seq = int(max(pairs["p_len"].max(), pairs["t_len"].max()))
+    max_seq = max(max_seq, SERVE_LMAX)
+    stride = wfe.reference_cigar_stride(SERVE_LMAX)
+    h_ascii = torch.empty(len(ascii), dtype=torch.uint8, pin_memory=True).numpy()
+    h_ascii[:] = ascii
+    reqs = [pairs[s:s + k] for s, k in zip(starts, sizes)]
+
+    # first tiers per length bucket, measured on a sample
+    ns = min(total, 200_000)
+    d_ascii = torch.from_numpy(ascii).cuda()
+    d_pairs = torch.from_numpy(pairs[:ns].view(np.uint8)).cuda()
+    buckets = SERVE_BUCKETS[:-1] + [max_seq]
+    with wfe.Context(max_seq_len=max_seq, batch_size=SERVE_MAX_PAIRS * 4, cigar_stride=stride) as c:
+        tiers = c.autotune(d_ascii, d_pairs, ns, buckets)
+    del d_ascii, d_pairs
+
+    outs = {m: (np.zeros(total, np.int32), np.zeros((total, stride), np.int8), np.zeros(total, np.uint8))
+            for m in ("served", "plain")}
+
+    def views(m, i):
+        d, c, st = outs[m]
+        s, k = starts[i], sizes[i]
+        return d[s:s + k], c[s:s + k], st[s:s + k]
+
+    srv = wfe.Server(max_seq_len=max_seq, cigar_stride=stride, lanes=4, memory_bytes=2 << 30,
+                     bucket_max_len=buckets, first_tier=tiers)
+    ctx = wfe.Context(max_seq_len=max_seq, batch_size=SERVE_MAX_PAIRS, cigar_stride=stride)
+    ctx.set_policy(buckets, tiers)
+
+    def serve(arrivals):
+        """Submit request i at arrivals[i] (monotonic ns); per-request latency in ms."""
+        handles = [None] * nreq
+        for i in range(nreq):
+            while True:
+                dt = arrivals[i] - time.monotonic_ns()
+                if dt <= 0:
+                    break
+                if dt > 200_000:
+                    time.sleep((dt - 100_000) / 1e9)
+            handles[i] = srv.submit(h_ascii, reqs[i], out=views("served", i))
+        for h in handles:
+            assert srv.poll(h)
+        done = np.array([h.info["done_ns"] for h in handles], dtype=np.float64)
+        return (done - arrivals) / 1e6, done.max()
+
+    def plain(arrivals):
+        lat = np.zeros(nreq)
+        last = 0
+        for i in range(nreq):
+            while time.monotonic_ns() < arrivals[i]:
+                dt = arrivals[i] - time.monotonic_ns()
+                if dt > 200_000:
+                    time.sleep((dt - 100_000) / 1e9)
+            ctx.align(h_ascii, reqs[i], out=views("plain", i))
+            last = time.monotonic_ns()
+            lat[i] = (last - arrivals[i]) / 1e6
+        return lat, last
+
+    # warm-up, then the peak: every request submitted at once
+    serve(np.full(nreq, time.monotonic_ns(), dtype=np.float64))
+    t0 = time.monotonic_ns()
+    _, t_end = serve(np.full(nreq, t0, dtype=np.float64))
+    peak = total / ((t_end - t0) / 1e9)
+    plain(np.full(nreq, time.monotonic_ns(), dtype=np.float64))
+    t0 = time.monotonic_ns()
+    _, t_end = plain(np.full(nreq, t0, dtype=np.float64))
+    plain_peak = total / ((t_end - t0) / 1e9)
+
+    rows = []
+    identical = True
+    for f in SERVE_RATES:
+        rate = f * peak / float(sizes.mean())  # requests per second
+        gaps = rng.exponential(1.0 / rate, nreq)
+        row = {"load": f, "offered_alignments_per_s": f * peak}
+        for m, fn in (("served", serve), ("plain", plain)):
+            base = time.monotonic_ns() + 2_000_000
+            arrivals = base + np.cumsum(gaps) * 1e9
+            lat, t_end = fn(arrivals)
+            row[m] = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                      "mean_ms": float(lat.mean()),
+                      "alignments_per_s": total / ((t_end - base) / 1e9)}
+        identical &= bool(np.array_equal(outs["served"][0], outs["plain"][0]) and
+                          np.array_equal(outs["served"][2], outs["plain"][2]))
+        rows.append(row)
+    # CIGARs of the two forms, up to each terminator
+    cs, cp = outs["served"][1], outs["plain"][1]
+    lens = np.argmax(cs == 0, axis=1)
+    same_cg = bool(np.array_equal(lens, np.argmax(cp == 0, axis=1)))
+    if same_cg:
+        mask = np.arange(stride)[None, :] <= lens[:, None]
+        same_cg = bool(np.array_equal(np.where(mask, cs, 0), np.where(mask, cp, 0)))
+    st = srv.stats()
+    srv.close()
+    ctx.close()
+    line = {"metric": "p50/p99 request latency and alignments/sec", "workload": "serve",
+            "unit": "ms / alignments/s",
+            "config": {"requests": nreq, "pairs": total, "request_pairs": f"log-uniform [1, {SERVE_MAX_PAIRS}]",
+                       "lengths": f"log-uniform [{SERVE_LMIN}, {SERVE_LMAX}]",
+                       "edit_prob": f"uniform [{SERVE_PMIN}, {SERVE_PMAX}]", "seed": SERVE_SEED,
+                       "arrivals": "Poisson", "lanes": 4, "memory_bytes": 2 << 30, "buckets": buckets,
+                       "first_tiers": tiers, "inputs": "pinned host memory"},
+            "peak_alignments_per_s": {"served": peak, "plain": plain_peak},
+            "rates": rows, "server": st,
+            "identical_results": identical and same_cg,
+            "all_ok": bool((outs["served"][2] == 0).all())}
+    print(json.dumps(line))
+    return 0 if line["identical_results"] and line["all_ok"] else 1
 
 
 def dist_env():
@@ -352,6 +489,8 @@ def main():
         return run_profile_case(args.profile_batch)
     if args.workload == "mixed":
         return run_mixed(args)
+    if args.workload == "serve":
+        return run_serve(args)
     if args.impl == "reference":
         return run_reference(args)
     import torch

@@ -30,7 +30,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-rdc=true", "-Xcompiler", "-fPI
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wextra", f"-I{INC}", f"-I{CSRC}"]
 CC_FLAGS = ["-O2", "-std=c11", "-fPIC", "-Wall", "-Wextra", "-ffp-contract=off", f"-I{INC}", f"-I{CSRC}"]
 
-LIB_CU = ["wfe_kernels.cu", "wfe_api.cu", "wfe_noalloc.cu"]
+LIB_CU = ["wfe_kernels.cu", "wfe_api.cu", "wfe_noalloc.cu", "wfe_server.cu"]
 LIB_CXX = ["wfe_host.cpp", "seqfile.cpp"]
 
 

@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "wfe.h"
+#include "wfe_internal.h"
 #include "wfe_kernels.cuh"
 
 using namespace wfe;
@@ -105,7 +106,7 @@ int fail_cuda(wfe_ctx* ctx, cudaError_t e)
 /* Device-side tier launches that failed (their pairs were left unaligned)
  * since the last call, reported once as a CUDA launch failure.  Read after
  * the work in question has completed. */
-int take_launch_error(wfe_ctx* ctx)
+int pop_launch_error(wfe_ctx* ctx)
 {
     volatile uint32_t* f = ctx->h_launch_error;
     if (!f || *f == 0u) return WFE_OK;
@@ -330,7 +331,14 @@ const char* wfe_strerror(int status)
 
 int wfe_last_cuda_error(const wfe_ctx* ctx) { return ctx ? ctx->last_cuda_error : g_last_create_error; }
 
-int wfe_create(const wfe_config* cfg, wfe_ctx** out)
+}  // extern "C"
+
+namespace wfe {
+int take_launch_error(wfe_ctx* ctx) { return pop_launch_error(ctx); }
+
+/* wfe_create with the slab budgets of tiers 5 and 6 (0: 2 GiB and 8 GiB):
+ * a smaller budget only lowers how many long pairs run at once. */
+int create_context(const wfe_config* cfg, uint64_t budget5, uint64_t budget6, wfe_ctx** out)
 {
     if (!cfg || !out) return WFE_ERR_INVALID_ARGUMENT;
     *out = nullptr;
@@ -379,7 +387,7 @@ int wfe_create(const wfe_config* cfg, wfe_ctx** out)
         } else if (t >= 5) {
             /* a slab per resident CTA (backtrace store, chain, runs; tier 6
              * also its wavefront), the grid trimmed to a budget */
-            const uint64_t budget = t == 5 ? (2ull << 30) : (8ull << 30);
+            const uint64_t budget = t == 5 ? (budget5 ? budget5 : (2ull << 30)) : (budget6 ? budget6 : (8ull << 30));
             const int grid = (int)std::min<uint64_t>((uint64_t)sh.grid, std::max<uint64_t>(1, budget / sh.slab));
             ctx->scratch_ctas[t] = grid;
             ctx->long_slab[t] = sh.slab;
@@ -407,9 +415,15 @@ int wfe_create(const wfe_config* cfg, wfe_ctx** out)
     *ctx->h_launch_error = 0u;
     if ((e = cudaHostGetDevicePointer(&ctx->d_launch_error, ctx->h_launch_error, 0)) != cudaSuccess) return bail(e);
     const size_t B = c.batch_size;
+    const bool host_calls = !(c.flags & WFE_FLAG_DEVICE_ONLY);
     for (auto& s : ctx->st) {
-        s.ascii_cap = B * 2u * (size_t)c.max_seq_len + 64u;
         if ((e = cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e);
+        /* a work list per length bucket and tier */
+        if ((e = cudaMalloc(&s.d_lists, kLists * B * sizeof(uint32_t))) != cudaSuccess) return bail(e);
+        if ((e = cudaMalloc(&s.d_counts, sizeof(uint32_t) * kCountWords)) != cudaSuccess) return bail(e);
+        if ((e = cudaMalloc(&s.d_pred, B * sizeof(uint16_t))) != cudaSuccess) return bail(e);
+        if (!host_calls) continue;
+        s.ascii_cap = B * 2u * (size_t)c.max_seq_len + 64u;
         if ((e = cudaMalloc(&s.d_ascii, s.ascii_cap)) != cudaSuccess) return bail(e);
         if ((e = cudaMalloc(&s.d_pairs, B * sizeof(wfe_pair))) != cudaSuccess) return bail(e);
         if ((e = cudaMalloc(&s.d_plen, B * sizeof(uint32_t))) != cudaSuccess) return bail(e);
@@ -417,14 +431,16 @@ int wfe_create(const wfe_config* cfg, wfe_ctx** out)
         if ((e = cudaMalloc(&s.d_dist, B * sizeof(int32_t))) != cudaSuccess) return bail(e);
         if ((e = cudaMalloc(&s.d_cigar, B * (size_t)c.cigar_stride + 16u)) != cudaSuccess) return bail(e);
         if ((e = cudaMalloc(&s.d_status, B)) != cudaSuccess) return bail(e);
-        /* a work list per length bucket and tier */
-        if ((e = cudaMalloc(&s.d_lists, kLists * B * sizeof(uint32_t))) != cudaSuccess) return bail(e);
-        if ((e = cudaMalloc(&s.d_counts, sizeof(uint32_t) * kCountWords)) != cudaSuccess) return bail(e);
-        if ((e = cudaMalloc(&s.d_pred, B * sizeof(uint16_t))) != cudaSuccess) return bail(e);
     }
     *out = ctx;
     return WFE_OK;
 }
+
+}  // namespace wfe
+
+extern "C" {
+
+int wfe_create(const wfe_config* cfg, wfe_ctx** out) { return wfe::create_context(cfg, 0, 0, out); }
 
 int wfe_set_policy(wfe_ctx* ctx, uint32_t nbuckets, const uint32_t* bucket_max_len, const int32_t* first_tier,
                    uint32_t flags)
@@ -533,7 +549,7 @@ int wfe_align_device(wfe_ctx* ctx, const char* d_ascii, const wfe_pair* d_pairs,
     if (max_len > ctx->cfg.max_seq_len) return WFE_ERR_SEQ_TOO_LONG;
     WFE_CUDA(ctx, cudaSetDevice(ctx->cfg.device));
     /* an earlier asynchronous call whose device-side launch failed */
-    if (const int r = take_launch_error(ctx)) return r;
+    if (const int r = pop_launch_error(ctx)) return r;
     cudaStream_t s = stream ? (cudaStream_t)stream : ctx->st[0].stream;
     const size_t B = ctx->cfg.batch_size;
     for (size_t b0 = 0; b0 < n; b0 += B) {
@@ -583,6 +599,7 @@ int align_host(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, in
                uint8_t* status_out)
 {
     const wfe_config& c = ctx->cfg;
+    if (c.flags & WFE_FLAG_DEVICE_ONLY) return WFE_ERR_INVALID_ARGUMENT;
     WFE_CUDA(ctx, cudaSetDevice(c.device));
     const bool want_cigar = cigar_out && c.cigar_stride;
 
@@ -712,7 +729,7 @@ int align_host(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, in
         ctx->stats.pairs += nb;
     }
     for (int i = 0; i < nstages; ++i) WFE_CUDA(ctx, cudaStreamSynchronize(ctx->st[i].stream));
-    return take_launch_error(ctx);
+    return pop_launch_error(ctx);
 }
 
 }  // namespace
@@ -953,7 +970,7 @@ extern "C" int wfe_autotune(wfe_ctx* ctx, const char* d_ascii, const wfe_pair* d
                 r = run_chain(ctx, st, L, m, d_dist, d_cigar, d_status, s, tiers);
                 cudaEventRecord(e1, s);
                 if (r != WFE_OK || cudaEventSynchronize(e1) != cudaSuccess) { r = WFE_ERR_CUDA; break; }
-                if ((r = take_launch_error(ctx)) != WFE_OK) break;
+                if ((r = pop_launch_error(ctx)) != WFE_OK) break;
                 float ms = 0.f;
                 cudaEventElapsedTime(&ms, e0, e1);
                 if (rep > 0) ms_min = std::min(ms_min, ms); /* the first run warms up */

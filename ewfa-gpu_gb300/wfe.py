@@ -25,6 +25,7 @@ PAIR_OK, PAIR_OVER_MAX_DISTANCE, PAIR_CIGAR_TRUNCATED, PAIR_TOO_LONG, PAIR_BAD_H
 PAIR_OUT_OF_RANGE = 5
 FLAG_NO_PIPELINE = 1
 FLAG_KERNEL_TIMING = 2
+FLAG_DEVICE_ONLY = 4
 POLICY_PREDICT = 1
 
 PAIR_DTYPE = np.dtype([("p_off", "<u8"), ("t_off", "<u8"), ("p_len", "<u4"), ("t_len", "<u4")])
@@ -36,6 +37,7 @@ SYMBOLS = [
     "wfe_cigar_from_history_device", "wfe_format_cigar", "wfe_check_cigar", "wfe_align_device_noalloc",
     "wfe_read_pair_file", "wfe_free_pair_file", "wfe_host_alloc", "wfe_host_free", "wfe_device_count",
     "wfe_device_name", "wfe_set_policy", "wfe_get_policy", "wfe_autotune",
+    "wfe_server_create", "wfe_server_destroy", "wfe_submit", "wfe_poll", "wfe_server_get_stats",
 ]
 NOALLOC_MAX_DISTANCE = 271
 NOALLOC_SCRATCH_BYTES = 16 << 20
@@ -57,6 +59,24 @@ class Stats(C.Structure):
                 ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("tier_entered", C.c_uint64 * 8),
                 ("tier_passed", C.c_uint64 * 8), ("tier_launches", C.c_uint64 * 8),
                 ("tier_ms", C.c_double * 8), ("mapped_batches", C.c_uint64)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int32), ("max_seq_len", C.c_uint32), ("cigar_stride", C.c_uint32),
+                ("max_distance", C.c_int32), ("lanes", C.c_uint32), ("batch_pairs", C.c_uint32),
+                ("memory_bytes", C.c_uint64), ("nbuckets", C.c_uint32), ("bucket_max_len", C.c_uint32 * 8),
+                ("first_tier", C.c_int32 * 8), ("policy_flags", C.c_uint32)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("submit_ns", C.c_uint64), ("start_ns", C.c_uint64), ("done_ns", C.c_uint64),
+                ("pairs", C.c_uint32), ("batches", C.c_uint32)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("requests", C.c_uint64), ("pairs", C.c_uint64), ("batches", C.c_uint64),
+                ("split_requests", C.c_uint64), ("max_in_flight", C.c_uint32), ("lanes", C.c_uint32),
+                ("memory_bytes", C.c_uint64), ("peak_memory", C.c_uint64)]
 
 
 class PairFileC(C.Structure):
@@ -114,6 +134,12 @@ def load() -> C.CDLL:
     L.wfe_host_free.restype = None
     L.wfe_device_count.argtypes = [C.POINTER(C.c_int)]
     L.wfe_device_name.argtypes = [C.c_int, C.c_char_p, sz, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.wfe_server_create.argtypes = [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]
+    L.wfe_server_destroy.argtypes = [vp]
+    L.wfe_server_destroy.restype = None
+    L.wfe_submit.argtypes = [vp, vp, sz, vp, sz, vp, vp, vp, C.POINTER(C.c_uint64)]
+    L.wfe_poll.argtypes = [vp, C.c_uint64, C.c_int64, C.POINTER(RequestInfo)]
+    L.wfe_server_get_stats.argtypes = [vp, C.POINTER(ServerStats)]
     for name in SYMBOLS:
         getattr(L, name)
     _lib = L
@@ -334,6 +360,91 @@ class Context:
         s = stream.cuda_stream if hasattr(stream, "cuda_stream") else (stream or 0)
         _check(load().wfe_align_device(self._h, _addr(d_ascii), _addr(d_pairs), n, max_len, _addr(d_dist),
                                        _addr(d_cigar), _addr(d_status), s), "wfe_align_device")
+
+
+# --------------------------------------------------------------------------
+# serving
+
+class Request:
+    """A submitted request: its ticket and the buffers its results go to."""
+    __slots__ = ("ticket", "ascii", "pairs", "dist", "cigar", "status", "info")
+
+    def __init__(self, ticket, ascii, pairs, dist, cigar, status):
+        self.ticket, self.ascii, self.pairs = ticket, ascii, pairs
+        self.dist, self.cigar, self.status = dist, cigar, status
+        self.info = None
+
+
+class Server:
+    """wfe_server: requests of any size submitted at any time, aligned in
+    continuously formed batches on several streams (see wfe_server_create)."""
+
+    def __init__(self, max_seq_len: int, cigar_stride: int = 0, max_distance: int = 0, lanes: int = 0,
+                 batch_pairs: int = 0, memory_bytes: int = 0, bucket_max_len=None, first_tier=None,
+                 predict: bool = False, device: int = 0):
+        cfg = ServerConfig()
+        cfg.device, cfg.max_seq_len, cfg.cigar_stride, cfg.max_distance = device, max_seq_len, cigar_stride, \
+            max_distance
+        cfg.lanes, cfg.batch_pairs, cfg.memory_bytes = lanes, batch_pairs, memory_bytes
+        if bucket_max_len:
+            cfg.nbuckets = len(bucket_max_len)
+            for i, m in enumerate(bucket_max_len):
+                cfg.bucket_max_len[i] = m
+                cfg.first_tier[i] = -1 if first_tier is None else first_tier[i]
+        cfg.policy_flags = POLICY_PREDICT if predict else 0
+        h = C.c_void_p()
+        _check(load().wfe_server_create(C.byref(cfg), C.byref(h)), "wfe_server_create")
+        self._h = h
+        self.cigar_stride = cigar_stride or reference_cigar_stride(max_seq_len)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            load().wfe_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def submit(self, ascii: np.ndarray, pairs: np.ndarray, out=None) -> Request:
+        """Queue a request; the arrays are kept alive by the returned Request."""
+        n = len(pairs)
+        pairs = np.ascontiguousarray(pairs, dtype=PAIR_DTYPE)
+        if out is None:
+            out = (np.zeros(n, np.int32), np.zeros((n, self.cigar_stride), np.int8), np.zeros(n, np.uint8))
+        dist, cg, st = out
+        t = C.c_uint64(0)
+        _check(load().wfe_submit(self._h, _addr(ascii), ascii.nbytes, _addr(pairs), n, _addr(dist), _addr(cg),
+                                 _addr(st), C.byref(t)), "wfe_submit")
+        return Request(t.value, ascii, pairs, dist, cg, st)
+
+    def poll(self, req: Request, timeout_us: int = -1) -> bool:
+        """True when the request has finished (req.info filled); False on timeout."""
+        info = RequestInfo()
+        rc = load().wfe_poll(self._h, req.ticket, timeout_us, C.byref(info))
+        if rc == ERR_TIMEOUT:
+            return False
+        _check(rc, "wfe_poll")
+        req.info = {"submit_ns": info.submit_ns, "start_ns": info.start_ns, "done_ns": info.done_ns,
+                    "pairs": info.pairs, "batches": info.batches}
+        return True
+
+    def poll_ticket(self, ticket: int, timeout_us: int = 0) -> int:
+        """Raw wfe_poll status of a ticket."""
+        return load().wfe_poll(self._h, ticket, timeout_us, None)
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        _check(load().wfe_server_get_stats(self._h, C.byref(s)), "wfe_server_get_stats")
+        return {k: getattr(s, k) for k, _ in ServerStats._fields_}
 
 
 def pack_device(d_ascii, d_pairs, n: int, d_words, words_per_seq: int, stream=None) -> None:

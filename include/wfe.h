@@ -93,6 +93,9 @@ typedef struct wfe_config {
 #define WFE_FLAG_NO_PIPELINE 1u   /* host calls: one batch in flight (no copy/compute overlap) */
 #define WFE_FLAG_KERNEL_TIMING 2u /* time every kernel launch with CUDA events on its
                                      stream; read back by wfe_get_stats */
+#define WFE_FLAG_DEVICE_ONLY 4u   /* no staging buffers for host calls: the context
+                                     serves wfe_align_device only (wfe_align and
+                                     wfe_align_strided return WFE_ERR_INVALID_ARGUMENT) */
 
 typedef struct wfe_ctx wfe_ctx;
 
@@ -289,6 +292,86 @@ int wfe_align_device_noalloc(const char* d_ascii, const wfe_pair* d_pairs, size_
                              uint32_t max_len, int32_t max_distance, int32_t* d_dist,
                              int8_t* d_cigar, uint32_t cigar_stride, uint8_t* d_status,
                              void* stream);
+
+/* ---- serving: continuous batching of requests ------------------------- */
+
+/* A request server on one GPU.  Requests of any size (1 pair and up) are
+ * submitted from any thread and answered asynchronously.  A scheduler thread
+ * admits waiting requests into a new device batch whenever one of `lanes`
+ * streams is free and the batch's bytes (sequences, descriptors, distances,
+ * statuses, CIGAR slots) fit in the free part of a device-memory arena of
+ * `memory_bytes`: a request that arrives while other batches run joins the
+ * next batch and its work overlaps theirs on the device; a request larger
+ * than what is free is split over several batches.  Each lane keeps its
+ * wavefront and backtrace scratch resident for the server's life.  Results
+ * do not depend on which requests share a batch.  The reference has no
+ * serving mode: its driver aligns one file in fixed batches
+ * (src/aligner.cu:40-71, src/wavefront.cu:173-208). */
+typedef struct wfe_server wfe_server;
+
+typedef struct wfe_server_config {
+    int32_t device;
+    uint32_t max_seq_len;       /* longest pattern or text of any request */
+    uint32_t cigar_stride;      /* bytes per CIGAR slot; 0 = as wfe_config */
+    int32_t max_distance;       /* 0 = no limit */
+    uint32_t lanes;             /* batches in flight at once, one stream each; 0 = 4 */
+    uint32_t batch_pairs;       /* pairs per batch at most; 0 = 65536 */
+    uint64_t memory_bytes;      /* device arena for batches in flight (and as much
+                                   page-locked host memory for their results);
+                                   0 = 2 GiB */
+    uint32_t nbuckets;          /* length buckets of every batch, as in
+                                   wfe_set_policy; 0 = one */
+    uint32_t bucket_max_len[WFE_MAX_BUCKETS];
+    int32_t first_tier[WFE_MAX_BUCKETS];
+    uint32_t policy_flags;      /* WFE_POLICY_* */
+} wfe_server_config;
+
+/* Times (steady clock, nanoseconds) and shape of one finished request. */
+typedef struct wfe_request_info {
+    uint64_t submit_ns;  /* wfe_submit was called */
+    uint64_t start_ns;   /* its first batch was enqueued */
+    uint64_t done_ns;    /* its last result was written to the caller's buffers */
+    uint32_t pairs;
+    uint32_t batches;    /* batches its pairs were spread over */
+} wfe_request_info;
+
+typedef struct wfe_server_stats {
+    uint64_t requests;        /* finished */
+    uint64_t pairs;           /* aligned */
+    uint64_t batches;         /* device batches run */
+    uint64_t split_requests;  /* requests spread over more than one batch */
+    uint32_t max_in_flight;   /* most batches on the device at once */
+    uint32_t lanes;
+    uint64_t memory_bytes;    /* arena size */
+    uint64_t peak_memory;     /* most arena bytes held at once */
+} wfe_server_stats;
+
+/* Create a server (one context per lane, created with WFE_FLAG_DEVICE_ONLY,
+ * the arena, and the scheduler thread).  WFE_ERR_BUSY when the device has
+ * less free memory than the arena asks for. */
+int wfe_server_create(const wfe_server_config* cfg, wfe_server** out);
+
+/* Finish every submitted request, then release everything. */
+void wfe_server_destroy(wfe_server* srv);
+
+/* Queue n pairs of ascii (ascii_bytes long; descriptors as in wfe_align) for
+ * alignment; outputs as in wfe_align.  Returns at once with *ticket.  The
+ * inputs and outputs must stay valid until wfe_poll reports the ticket
+ * finished.  Checked here: every pair lies inside ascii
+ * (WFE_ERR_INVALID_ARGUMENT) and is at most max_seq_len long
+ * (WFE_ERR_SEQ_TOO_LONG); nothing is queued then. */
+int wfe_submit(wfe_server* srv, const char* ascii, size_t ascii_bytes, const wfe_pair* pairs,
+               size_t n, int32_t* dist_out, int8_t* cigar_out, uint8_t* status_out,
+               uint64_t* ticket);
+
+/* Wait up to timeout_us microseconds (0: do not wait, < 0: no limit) for a
+ * request.  WFE_OK: finished and its results written; the ticket is retired
+ * and info (may be NULL) filled.  WFE_ERR_TIMEOUT: not finished yet.
+ * WFE_ERR_NOT_FOUND: unknown or already retired ticket.  A request whose
+ * batch failed returns that error (WFE_ERR_CUDA) and is retired too. */
+int wfe_poll(wfe_server* srv, uint64_t ticket, int64_t timeout_us, wfe_request_info* info);
+
+int wfe_server_get_stats(wfe_server* srv, wfe_server_stats* out);
 
 /* ---- host helpers --------------------------------------------------------- */
 

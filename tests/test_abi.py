@@ -107,3 +107,34 @@ def test_check_rejects_bad_cigars():
     assert not wfe.check_cigar(p, t, np.array([-3, ord("X"), 0], np.int8))[0]    # X on a match
     assert not wfe.check_cigar(p, t, np.array([-5, 0], np.int8))[0]              # past the end
     assert not wfe.check_cigar(p, t, np.array([ord("Q"), 0], np.int8))[0]        # unknown letter
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes mirrors of the ABI structs have the C sizes and offsets."""
+    import ctypes as C
+    import subprocess
+    src = tmp_path / "layout.c"
+    checks = {
+        "wfe_config": (wfe.Config, ["device", "max_seq_len", "batch_size", "max_distance", "cigar_stride", "flags"]),
+        "wfe_stats": (wfe.Stats, ["pairs", "tier_entered", "tier_ms", "mapped_batches"]),
+        "wfe_server_config": (wfe.ServerConfig, ["memory_bytes", "nbuckets", "bucket_max_len", "first_tier",
+                                                 "policy_flags"]),
+        "wfe_request_info": (wfe.RequestInfo, ["submit_ns", "done_ns", "pairs", "batches"]),
+        "wfe_server_stats": (wfe.ServerStats, ["split_requests", "max_in_flight", "lanes", "peak_memory"]),
+        "wfe_pair_file": (wfe.PairFileC, ["ascii_bytes", "n", "longest", "pinned"]),
+    }
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "wfe.h"', "int main(void) {"]
+    for name, (_, fields) in checks.items():
+        lines.append(f'printf("%zu\\n", sizeof({name}));')
+        lines += [f'printf("%zu\\n", offsetof({name}, {f}));' for f in fields]
+    lines.append("return 0; }")
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], stdout=subprocess.PIPE, text=True,
+                                          check=True).stdout.split()]
+    want = []
+    for name, (cls, fields) in checks.items():
+        want.append(C.sizeof(cls))
+        want += [getattr(cls, f).offset for f in fields]
+    assert got == want
