@@ -42,12 +42,27 @@ import numpy as np  # noqa: E402
 
 import wfe  # noqa: E402
 
-PAIRS, BATCH, LENGTH, EDIT_P, SEED = 1_000_000, 100_000, 150, 0.05, 2
 METRIC = "alignments/sec"
-WORKLOAD = (f"short reads: {PAIRS:,} pairs x {LENGTH} bases, edit probability {EDIT_P}, "
-            f"batches of {BATCH:,}; distance + full CIGAR per pair")
-CIGAR_STRIDE = wfe.reference_cigar_stride(LENGTH)   # the reference's cigar_max_len for -l 150
-MAX_SEQ_LEN = 2 * LENGTH                             # the reference reader's slot holds 2*l bases
+# fixed-length throughput workloads: pairs, batch, length, edit probability,
+# seed, committed ncu summary of the dominant kernel
+THROUGHPUT = {
+    "short": (1_000_000, 100_000, 150, 0.05, 2, "tier0_short_reads.txt"),
+    "long": (200_000, 20_000, 1000, 0.10, 3, "long_reads.txt"),
+}
+
+
+def select_workload(name: str) -> None:
+    """Set the module's workload constants (the short-read workload unless
+    another is asked for)."""
+    global PAIRS, BATCH, LENGTH, EDIT_P, SEED, PROFILE, WORKLOAD, CIGAR_STRIDE, MAX_SEQ_LEN
+    PAIRS, BATCH, LENGTH, EDIT_P, SEED, PROFILE = THROUGHPUT[name]
+    WORKLOAD = (f"{name} reads: {PAIRS:,} pairs x {LENGTH} bases, edit probability {EDIT_P}, "
+                f"batches of {BATCH:,}; distance + full CIGAR per pair")
+    CIGAR_STRIDE = wfe.reference_cigar_stride(LENGTH)   # the reference's cigar_max_len for -l LENGTH
+    MAX_SEQ_LEN = 2 * LENGTH                             # the reference reader's slot holds 2*l bases
+
+
+select_workload("short")
 
 
 def parse():
@@ -57,37 +72,86 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["short", "mixed", "serve"], default="short",
+    ap.add_argument("--workload", choices=["short", "long", "mixed", "serve"], default="short",
                     help="short: the short-read throughput workload (the metric's configuration); "
+                         "long: 200,000 pairs of 1,000 bases at edit probability 0.10; "
                          "mixed: uneven lengths, plain fixed-shape launches vs length buckets; "
                          "serve: Poisson request stream, the request server vs one call per request")
     ap.add_argument("--requests", type=int, default=0, help="serve workload: number of requests (default 1,000)")
     ap.add_argument("--pairs", type=int, default=0, help="mixed workload: number of pairs (default 2,000,000)")
     ap.add_argument("--profile-batch", type=int, default=0,
-                    help="profiling case: align this many pairs of the workload as ONE batch, twice "
-                         "(a warm-up chain, then the chain to capture), and exit")
+                    help="profiling case: run the --profile-kernel kernels twice over ONE batch of this "
+                         "many pairs of the workload (a warm-up, then the launch to capture), and exit")
+    ap.add_argument("--profile-kernel", choices=["tier", "aux"], default="tier")
+    ap.add_argument("--profile-first-tier", type=int, default=-1)
     return ap.parse_args()
 
 
-def run_profile_case(n: int) -> int:
-    """One batch of n pairs through wfe_align_device, twice.  For ncu: the
-    second chain's tier-0 launch is the 6th tier_kernel launch (-s 5 -c 1)."""
+def histories_from_cigars(cg: np.ndarray) -> np.ndarray:
+    """The reference's 128-bit history of each pair (two uint64 words): the
+    operation of score step d (X = 2, I = 1, D = 3) in 2-bit field d - 1,
+    fields 0-31 in the first word (src/kernels.cu:154-171)."""
+    code = np.zeros(256, np.uint64)
+    code[ord("X")], code[ord("I")], code[ord("D")] = 2, 1, 3
+    b = cg.view(np.uint8)
+    term = np.cumsum(b == 0, axis=1) > 0
+    op = np.where(term | (cg <= 0), 0, code[b])
+    idx = np.cumsum(op > 0, axis=1) - 1
+    words = np.zeros((len(cg), 2), np.uint64)
+    for w in range(2):
+        sel = (op > 0) & (idx // 32 == w)
+        sh = (2 * (idx % 32)).astype(np.uint64)
+        words[:, w] = np.where(sel, op << sh, 0).sum(axis=1, dtype=np.uint64)
+    return words
+
+
+def run_profile_case(args) -> int:
+    """Profiling cases: every kernel runs twice over one batch of n pairs of
+    the workload (the first launch warms up, ncu captures the second):
+      tier     the alignment chain from its first tier (--profile-first-tier)
+      aux      wfe_pack_device, the distance-prediction and routing kernels of
+               a bucketed batch, and the CIGAR-from-history kernel fed the
+               histories of this workload's alignments."""
     import torch
     torch.cuda.set_device(0)
+    n = args.profile_batch
     ascii, pairs = wfe.generate(n, LENGTH, p_min=EDIT_P, seed=SEED)
     d_ascii = torch.from_numpy(ascii).cuda()
     d_pairs = torch.from_numpy(pairs.view(np.uint8)).cuda()
     d_dist = torch.zeros(n, dtype=torch.int32, device="cuda")
     d_cigar = torch.zeros(n * CIGAR_STRIDE, dtype=torch.int8, device="cuda")
     d_status = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    out = {"profile_batch": n, "kernel": args.profile_kernel}
     with wfe.Context(max_seq_len=MAX_SEQ_LEN, batch_size=n, cigar_stride=CIGAR_STRIDE) as ctx:
-        for _ in range(2):
-            ctx.align_device(d_ascii, d_pairs, n, MAX_SEQ_LEN, d_dist, d_cigar, d_status)
+        if args.profile_kernel == "tier":
+            if args.profile_first_tier >= 0:
+                ctx.set_policy([MAX_SEQ_LEN], [args.profile_first_tier])
+            for _ in range(2):
+                ctx.align_device(d_ascii, d_pairs, n, MAX_SEQ_LEN, d_dist, d_cigar, d_status)
+                torch.cuda.synchronize()
+            out["tier_launches"] = ctx.stats()["tier_launches"][:7]
+            out["tier_passed"] = ctx.stats()["tier_passed"][:7]
+        else:
+            wps = (MAX_SEQ_LEN + 15) // 16
+            d_words = torch.zeros(2 * n * wps, dtype=torch.int32, device="cuda")
+            for _ in range(2):
+                wfe.pack_device(d_ascii, d_pairs, n, d_words, wps)
+            ctx.set_policy([LENGTH // 2, MAX_SEQ_LEN], [0, 0], predict=True)
+            for _ in range(2):
+                ctx.align_device(d_ascii, d_pairs, n, MAX_SEQ_LEN, d_dist, d_cigar, d_status)
             torch.cuda.synchronize()
-        launches = ctx.stats()["tier_launches"][:5]
+            cg = d_cigar.view(n, CIGAR_STRIDE).cpu().numpy()
+            d_hist = torch.from_numpy(histories_from_cigars(cg).view(np.int64).reshape(-1)).cuda()
+            d_cg2 = torch.zeros_like(d_cigar)
+            d_st2 = torch.zeros_like(d_status)
+            for _ in range(2):
+                wfe.cigar_from_history_device(d_ascii, d_pairs, n, MAX_SEQ_LEN, d_dist, d_hist, d_cg2,
+                                              CIGAR_STRIDE, d_st2)
+            torch.cuda.synchronize()
+            out["history_cigars_equal"] = bool(torch.equal(d_cg2, d_cigar))
     mb = (len(ascii) + n * (CIGAR_STRIDE + 29)) / 2**20
-    print(json.dumps({"profile_batch": n, "device_MiB": round(mb, 1), "tier_launches": launches,
-                      "status_ok": bool((d_status.cpu().numpy() == 0).all())}))
+    out.update({"device_MiB": round(mb, 1), "status_ok": bool((d_status.cpu().numpy() == 0).all())})
+    print(json.dumps(out))
     return 0
 
 
@@ -387,7 +451,7 @@ def measured_hbm_peak():
 def profiled_traffic():
     """DRAM bytes per launch of the dominant kernel from the committed ncu
     summary, if one records it (a line 'traffic_bytes_per_launch: N')."""
-    p = os.path.join(ROOT, "profiles", "tier0_short_reads.txt")
+    p = os.path.join(ROOT, "profiles", PROFILE)
     try:
         for line in open(p):
             if line.startswith("traffic_bytes_per_launch:"):
@@ -431,8 +495,8 @@ def reference_cuda_baseline():
         oracle.build(ref=False)
     except Exception:
         return None
-    if not oracle.ref_cuda_available():
-        return None
+    if not oracle.ref_cuda_available() or LENGTH != 150:
+        return None  # the reference searches distances up to 63: only the short-read workload fits
     runs = {}
     for t in (1, 2, 4, 8):
         rec = oracle.ref_cuda_run(PAIRS, LENGTH, EDIT_P, SEED, batch=BATCH, threads=t, reps=3)
@@ -485,12 +549,13 @@ def run_reference(args):
 
 def main():
     args = parse()
-    if args.profile_batch:
-        return run_profile_case(args.profile_batch)
     if args.workload == "mixed":
         return run_mixed(args)
     if args.workload == "serve":
         return run_serve(args)
+    select_workload(args.workload)
+    if args.profile_batch:
+        return run_profile_case(args)
     if args.impl == "reference":
         return run_reference(args)
     import torch
@@ -589,6 +654,10 @@ def main():
     # bytes that crossed the CPU-GPU link per step: staged copies (counted by
     # the library) plus what the kernels read/wrote in place in pinned memory
     in_place = st2["mapped_batches"] == st2["batches"]
+    # with pinned buffers the kernels read each batch's descriptors and
+    # sequences in place and write distances, statuses and the used bytes of
+    # each CIGAR slot (rounded to 4) in place: those are the bytes that cross
+    # the CPU-GPU link; staged calls count their copies in the statistics
     if in_place:
         h2d = int(pairs["p_len"].sum() + pairs["t_len"].sum()) // nb + BATCH * pair_bytes
         out_len = np.minimum((cigar_lengths(h_cigar) + 4) // 4 * 4, CIGAR_STRIDE)
@@ -617,11 +686,14 @@ def main():
             "data": "synthetic (seeded generator; no dataset)",
             "config": {"workload": WORKLOAD, "pairs_per_gpu": PAIRS, "batch": BATCH, "length": LENGTH,
                        "edit_prob": EDIT_P, "seed": SEED, "cigar_stride": CIGAR_STRIDE,
-                       "l2": "inputs larger than L2: steps cycle over 10 batches (300 MB ASCII, 152 MB CIGAR slots)",
+                       "l2": (f"inputs larger than L2: steps cycle over {nb} batches "
+                              f"({len(ascii) / 1e6:.0f} MB ASCII, {PAIRS * CIGAR_STRIDE / 1e6:.0f} MB CIGAR slots)"),
                        "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": f"tier_kernel tier {top}", "alg_bytes_per_launch": alg_bytes,
+                         "kernel": f"tier_kernel tier {top}" + (" and the tiers it hands pairs on to (one timed "
+                                                                     "chain)" if any(st["tier_passed"]) else ""),
+                         "alg_bytes_per_launch": alg_bytes,
                          "launch_ms": launch_ms},
             "gcups": {"value": value * cells_per_pair / 1e9,
                       "definition": "equivalent DP cell updates: sum of p_len * t_len per second / 1e9"},
@@ -630,8 +702,8 @@ def main():
             "e2e": e2e,
             "gpu_launches": gpu_launches,
             "clocks": clocks.summary(),
-            "tiers": {"launches": st["tier_launches"][:5], "ms": [round(x, 4) for x in tier_ms[:5]],
-                      "passed_on": st["tier_passed"][:5]},
+            "tiers": {"launches": st["tier_launches"][:7], "ms": [round(x, 4) for x in tier_ms[:7]],
+                      "passed_on": st["tier_passed"][:7]},
         }
         print(json.dumps(line))
     ctx.close()

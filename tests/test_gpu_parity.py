@@ -318,6 +318,28 @@ def test_pinned_buffers_read_and_written_in_place():
     compare_with_oracle(ascii, pairs, stride, *want)
 
 
+def test_pinned_pairs_in_any_order():
+    """Pinned descriptor layout read in place: pairs swapped in from far
+    away, and batches whose first pair lies after their last, give the same
+    results as the staged path."""
+    torch_cuda()
+    ascii, pairs = wfe.generate(20000, 150, p_min=0.05, seed=16)
+    rng = np.random.default_rng(16)
+    order = np.arange(len(pairs))
+    a, b = rng.choice(len(pairs), 300, replace=False), rng.choice(len(pairs), 300, replace=False)
+    order[a], order[b] = order[b], order[a]
+    order[5000:6000] = order[5000:6000][::-1]   # first pair of a batch after its last
+    mixed = pairs[order]
+    with wfe.Context(max_seq_len=300, batch_size=3000, cigar_stride=152) as ctx:
+        want = ctx.align(ascii, mixed)
+        got = ctx.align(_pinned(ascii), _pinned(mixed))
+        assert ctx.stats()["mapped_batches"] > 0
+    np.testing.assert_array_equal(got[0], want[0])
+    np.testing.assert_array_equal(got[2], want[2])
+    assert_same_cigars(got[1], want[1])
+    compare_with_oracle(ascii, mixed, 152, *want)
+
+
 def test_pinned_bad_descriptors_flagged_per_pair():
     """In place, a descriptor outside the buffer or a sequence over
     max_seq_len is reported per pair; nothing outside the buffer is read."""
