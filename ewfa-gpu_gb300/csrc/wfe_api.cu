@@ -198,6 +198,16 @@ TimedLaunch* begin_timing(wfe_ctx* ctx, int t, cudaStream_t s, int* rc)
     return &ctx->timed.back();
 }
 
+/* Last tier of a chain from tier `first`: a distance cap at or below a
+ * tier's capacity ends the chain there. */
+int chain_end(const wfe_config& c, int first, int last)
+{
+    if (c.max_distance > 0)
+        for (int u = first; u <= last; ++u)
+            if (c.max_distance <= tier_info(u).dcap) return u;
+    return last;
+}
+
 /* Launch the first tier of one bucket's chain over `work` (NULL: pairs
  * 0..n-1); the last CTA of every tier starts the next tier with work, on the
  * device. */
@@ -224,11 +234,7 @@ int launch_bucket(wfe_ctx* ctx, Stage& st, const BucketPlan& bp, int bucket_inde
     a.ops_scratch = ctx->d_ops_scratch;
     a.ops_scratch_bytes = ctx->ops_scratch_bytes;
     a.tier = t;
-    /* a distance cap at or below a tier's capacity ends the chain there */
-    int last = bp.last_tier;
-    if (c.max_distance > 0)
-        for (int u = t; u <= bp.last_tier; ++u)
-            if (c.max_distance <= tier_info(u).dcap) { last = u; break; }
+    const int last = chain_end(c, t, bp.last_tier);
     a.chain.last_tier = last;
     for (int u = 0; u < kNumTiers; ++u) {
         a.chain.shape[u] = bp.shape[u];
@@ -281,7 +287,8 @@ int run_chain(wfe_ctx* ctx, Stage& st, const Layout& L, uint32_t n, int32_t* dis
     for (int b = 0; b < ctx->nbuckets; ++b) {
         bk.max_len[b] = ctx->bucket[b].max_len;
         bk.first_tier[b] = first_override ? first_override[b] : ctx->bucket[b].first_tier;
-        bk.last_tier[b] = ctx->bucket[b].last_tier;
+        /* routing never goes past the end of the bucket's chain */
+        bk.last_tier[b] = chain_end(ctx->cfg, bk.first_tier[b], ctx->bucket[b].last_tier);
     }
     for (int t = 0; t < kNumTiers; ++t) bk.dcap[t] = tier_info(t).dcap;
     /* predictions only move pairs of buckets that start below tier 5 */

@@ -133,9 +133,19 @@ size_t cta_smem_bytes(uint32_t max_len, uint32_t cigar_stride)
     return group_smem_bytes<T>(max_len, cigar_stride) * (size_t)(kWarps * T::GPW);
 }
 
+/* The alignment kernel of a tier, in two forms with one body (tier_body):
+ *   tier_kernel_bounded<T, PREDICT>  the 4-lane tier 0 and the prediction
+ *       pass, launched from the host only, with launch bounds that set its
+ *       register budget for 8 resident CTAs per SM;
+ *   tier_kernel<T>  the tiers 1-4 that chains launch from the device, with
+ *       no launch bounds: a grid launched from the device whose kernel
+ *       declares launch bounds and uses dynamic shared memory was measured
+ *       to run one CTA per SM at a time, whatever the bounds say. */
 template <class T, bool PREDICT = false>
 __global__ void __launch_bounds__(kThreads, T::MINB)
-tier_kernel(AlignLaunch A, uint32_t seq_words, uint32_t gbytes);
+tier_kernel_bounded(const __grid_constant__ AlignLaunch A, uint32_t seq_words, uint32_t gbytes);
+template <class T>
+__global__ void tier_kernel(const __grid_constant__ AlignLaunch A, uint32_t seq_words, uint32_t gbytes);
 
 /* Tier 0 carries the short-read workloads; its shape is tuned on the GPU
  * (4 lanes per pair, 11 chunks, 8 resident CTAs per SM by default). */
@@ -147,56 +157,84 @@ tier_kernel(AlignLaunch A, uint32_t seq_words, uint32_t gbytes);
 #endif
 using T0 = Tier<4, WFE_T0_J, true, 5, WFE_T0_MINB>; /* distance <= 4*J + 1 (21) */
 
+/* launched from the device too: no launch bounds (see tier_kernel) */
 template <bool GLOBAL_WF>
-__global__ void __launch_bounds__(kLongThreads) long_kernel(AlignLaunch A);
+__global__ void long_kernel(const __grid_constant__ AlignLaunch A);
 using T1 = Tier<32, 2, true, 1>;   /* distance <= 79  */
 using T2 = Tier<32, 4, true, 1>;   /* distance <= 143 */
 using T3 = Tier<32, 8, false, 1>;  /* distance <= 271 */
 using T4 = Tier<32, 16, false, 1>; /* distance <= 527 */
 
-template <class T>
-__device__ void launch_on_device(const AlignLaunch& a, uint32_t count)
+/* Tail launch of tier u over its list of `count` pairs, built in the launch's
+ * own parameter buffer: A (a __grid_constant__ kernel parameter, read in
+ * place) is copied word by word and the per-tier fields are patched.  No
+ * copy of the launch record is made on the stack -- a kernel whose code
+ * holds a large stack frame keeps only a few CTAs resident per SM, and that
+ * limit is also what a grid launched from the device runs with. */
+template <typename K>
+__device__ __forceinline__ void tail_launch(K kernel, const AlignLaunch& A, int u, int grid, int threads,
+                                            uint32_t smem, bool tier_args, uint32_t seq_words, uint32_t gbytes)
 {
-    const TierShape& sh = a.chain.shape[a.tier];
+    void* buf = cudaGetParameterBufferV2((void*)kernel, dim3((unsigned)grid), dim3((unsigned)threads), smem);
+    if (!buf) {
+        if (A.chain.launch_error) atomicOr_system(A.chain.launch_error, 1u << u);
+        return;
+    }
+    const unsigned long long* src = reinterpret_cast<const unsigned long long*>(&A);
+    unsigned long long* dst = static_cast<unsigned long long*>(buf);
+    static_assert(sizeof(AlignLaunch) % 8 == 0, "launch record is copied in 8-byte words");
+#pragma unroll 4
+    for (unsigned i = 0; i < sizeof(AlignLaunch) / 8; ++i) dst[i] = src[i];
+    AlignLaunch* n = static_cast<AlignLaunch*>(buf);
+    n->tier = u;
+    n->work = A.chain.list[u];
+    n->work_count = A.chain.counts + u;
+    n->retry = u < A.chain.last_tier ? A.chain.list[u + 1] : nullptr;
+    n->retry_count = A.chain.counts + u + 1;
+    n->passed_total = A.chain.passed ? A.chain.passed + u : nullptr;
+    if (tier_args) {
+        uint32_t* extra = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(buf) + sizeof(AlignLaunch));
+        extra[0] = seq_words;
+        extra[1] = gbytes;
+    }
+    if (cudaLaunchDeviceV2(buf, cudaStreamTailLaunch) != cudaSuccess) {
+        if (A.chain.launch_error) atomicOr_system(A.chain.launch_error, 1u << u);
+        return;
+    }
+    if (A.chain.launched) atomicAdd(A.chain.launched + u, 1ull);
+}
+
+template <class T>
+__device__ __forceinline__ void launch_on_device(const AlignLaunch& A, int u, uint32_t count)
+{
+    const TierShape& sh = A.chain.shape[u];
     const uint32_t per_cta = (uint32_t)(kWarps * T::GPW);
     const int grid = max(1, min(sh.grid, (int)((count + per_cta - 1u) / per_cta)));
-    tier_kernel<T><<<grid, kThreads, sh.smem, cudaStreamTailLaunch>>>(a, sh.seq_words, sh.gbytes);
+    static_assert(T::G == 32, "only the 32-lane tiers are launched from the device");
+    tail_launch(tier_kernel<T>, A, u, grid, kThreads, sh.smem, true, sh.seq_words, sh.gbytes);
 }
 
 /* Called by the last CTA of tier A.tier: tier u (> A.tier) runs over its
  * list of `count` pairs once this grid has completed. */
-__device__ __noinline__ void launch_tier_on_device(const AlignLaunch& A, int u, uint32_t count)
+__device__ void launch_tier_on_device(const AlignLaunch& A, int u, uint32_t count)
 {
-    AlignLaunch n = A;
-    n.tier = u;
-    n.work = A.chain.list[u];
-    n.work_count = A.chain.counts + u;
-    n.retry = u < A.chain.last_tier ? A.chain.list[u + 1] : nullptr;
-    n.retry_count = A.chain.counts + u + 1;
-    n.passed_total = A.chain.passed ? A.chain.passed + u : nullptr;
     switch (u) {
-    case 1: launch_on_device<T1>(n, count); break;
-    case 2: launch_on_device<T2>(n, count); break;
-    case 3: launch_on_device<T3>(n, count); break;
-    case 4: launch_on_device<T4>(n, count); break;
+    case 1: launch_on_device<T1>(A, u, count); break;
+    case 2: launch_on_device<T2>(A, u, count); break;
+    case 3: launch_on_device<T3>(A, u, count); break;
+    case 4: launch_on_device<T4>(A, u, count); break;
     case 5:
     case 6: {
-        const TierShape& sh = n.chain.shape[u];
+        const TierShape& sh = A.chain.shape[u];
         const int grid = max(1, min(sh.grid, (int)count));
         if (u == 5)
-            long_kernel<false><<<grid, kLongThreads, sh.smem, cudaStreamTailLaunch>>>(n);
+            tail_launch(long_kernel<false>, A, u, grid, kLongThreads, sh.smem, false, 0u, 0u);
         else
-            long_kernel<true><<<grid, kLongThreads, sh.smem, cudaStreamTailLaunch>>>(n);
+            tail_launch(long_kernel<true>, A, u, grid, kLongThreads, sh.smem, false, 0u, 0u);
         break;
     }
     default: return;
     }
-    if (cudaGetLastError() != cudaSuccess) {
-        /* the pairs of tier u and above stay unaligned: tell the host */
-        if (n.chain.launch_error) atomicOr_system(n.chain.launch_error, 1u << u);
-        return;
-    }
-    if (n.chain.launched) atomicAdd(n.chain.launched + u, 1ull);
 }
 
 /* End of a tier kernel: the last CTA to finish starts the next tier that has
@@ -222,8 +260,7 @@ __device__ __forceinline__ void chain_next(const AlignLaunch& A)
 }
 
 template <class T, bool PREDICT>
-__global__ void __launch_bounds__(kThreads, T::MINB)
-tier_kernel(AlignLaunch A, uint32_t seq_words, uint32_t gbytes)
+__device__ __forceinline__ void tier_body(const AlignLaunch& A, uint32_t seq_words, uint32_t gbytes)
 {
     constexpr int G = T::G, J = T::J, NC = T::NC, DCAP = T::DCAP, GPW = T::GPW;
     using OE = typename T::OE;
@@ -416,6 +453,19 @@ tier_kernel(AlignLaunch A, uint32_t seq_words, uint32_t gbytes)
     if constexpr (!PREDICT) chain_next(A);
 }
 
+template <class T, bool PREDICT>
+__global__ void __launch_bounds__(kThreads, T::MINB)
+tier_kernel_bounded(const __grid_constant__ AlignLaunch A, uint32_t seq_words, uint32_t gbytes)
+{
+    tier_body<T, PREDICT>(A, seq_words, gbytes);
+}
+
+template <class T>
+__global__ void tier_kernel(const __grid_constant__ AlignLaunch A, uint32_t seq_words, uint32_t gbytes)
+{
+    tier_body<T, false>(A, seq_words, gbytes);
+}
+
 /* ------------------------------------------------------------------------ */
 /* Tiers 5 and 6: one CTA of 256 threads per pair, for distances beyond the
  * register tiers.  Step d computes the 2d+1 cells of [-d, d] in 32-cell
@@ -438,7 +488,7 @@ __host__ __device__ __forceinline__ uint64_t long_row(int d)
 }
 
 template <bool GLOBAL_WF>
-__global__ void __launch_bounds__(kLongThreads) long_kernel(AlignLaunch A)
+__global__ void long_kernel(const __grid_constant__ AlignLaunch A)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr int kW = kLongThreads / 32;
@@ -609,16 +659,25 @@ const TierInfo kTiers[kNumTiers] = {
     {kLongThreads, 0, 0x7fffffff, false},
 };
 
+/* The kernel a tier's host launches use (see tier_kernel_bounded). */
+template <class T>
+const void* host_kernel()
+{
+    if constexpr (T::G == 32) return (const void*)tier_kernel<T>;
+    else return (const void*)tier_kernel_bounded<T, false>;
+}
+
 template <class T>
 TierShape shape_of(uint32_t max_len, uint32_t cigar_stride, int sm_count)
 {
     TierShape sh{};
     const size_t smem = cta_smem_bytes<T>(max_len, cigar_stride);
     if (smem > 227u * 1024u) return sh;
-    if (allow_smem((const void*)tier_kernel<T>, smem) != cudaSuccess)
+    const void* fn = host_kernel<T>();
+    if (allow_smem(fn, smem) != cudaSuccess)
         return sh;
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, tier_kernel<T>, kThreads, smem) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kThreads, smem) != cudaSuccess)
         return sh;
     sh.grid = std::max(1, nb) * sm_count;
     sh.smem = (uint32_t)smem;
@@ -642,9 +701,12 @@ cudaError_t launch(const AlignLaunch& a, int grid, cudaStream_t s)
     if (smem > 227u * 1024u) return cudaErrorInvalidValue;
     if (!T::SMEM_OPS && a.ops_scratch_bytes < T::ops_bytes * (size_t)grid * (kWarps * T::GPW))
         return cudaErrorInvalidValue;
-    cudaError_t e = allow_smem((const void*)tier_kernel<T>, smem);
+    cudaError_t e = allow_smem(host_kernel<T>(), smem);
     if (e != cudaSuccess) return e;
-    tier_kernel<T><<<grid, kThreads, smem, s>>>(a, sw, (uint32_t)gb);
+    if constexpr (T::G == 32)
+        tier_kernel<T><<<grid, kThreads, smem, s>>>(a, sw, (uint32_t)gb);
+    else
+        tier_kernel_bounded<T><<<grid, kThreads, smem, s>>>(a, sw, (uint32_t)gb);
     return cudaGetLastError();
 }
 
@@ -883,7 +945,7 @@ cudaError_t launch_predict(const Layout& L, uint32_t n, uint32_t max_len, uint16
     const uint32_t plen = std::min<uint32_t>(max_len, (uint32_t)kPredictPrefix);
     const size_t gb = group_smem_bytes<T0>(plen, 0);
     const size_t smem = gb * (size_t)(kWarps * T0::GPW);
-    cudaError_t e = allow_smem((const void*)tier_kernel<T0, true>, smem);
+    cudaError_t e = allow_smem((const void*)tier_kernel_bounded<T0, true>, smem);
     if (e != cudaSuccess) return e;
     AlignLaunch a{};
     a.L = L;
@@ -893,7 +955,7 @@ cudaError_t launch_predict(const Layout& L, uint32_t n, uint32_t max_len, uint16
     a.tier = 0;
     const uint32_t per_cta = kWarps * T0::GPW;
     grid = std::max(1, std::min(grid, (int)((n + per_cta - 1) / per_cta)));
-    tier_kernel<T0, true><<<grid, kThreads, smem, s>>>(a, seq_words_for(plen), (uint32_t)gb);
+    tier_kernel_bounded<T0, true><<<grid, kThreads, smem, s>>>(a, seq_words_for(plen), (uint32_t)gb);
     return cudaGetLastError();
 }
 

@@ -434,6 +434,19 @@ def test_length_buckets_same_results():
     compare_with_oracle(ascii, pairs, 2048, *one)
 
 
+def test_length_buckets_with_distance_cap():
+    """With max_distance, routing (by bucket and by prediction) never sends
+    a pair past the tier where the capped chain ends."""
+    torch_cuda()
+    ascii, pairs = wfe.generate(4000, 100, 1500, p_min=0.01, p_max=0.15, seed=19)
+    with wfe.Context(max_seq_len=1700, cigar_stride=1024, max_distance=63) as ctx:
+        for predict in (False, True):
+            ctx.set_policy([256, 512, 1700], [0, 0, 0], predict=predict)
+            got = ctx.align(ascii, pairs)
+            assert (got[2] == wfe.PAIR_OVER_MAX_DISTANCE).any() and (got[2] == wfe.PAIR_OK).any()
+            compare_with_oracle(ascii, pairs, 1024, *got, max_distance=63)
+
+
 def test_autotune_installs_and_caches(tmp_path):
     torch = torch_cuda()
     ascii, pairs = wfe.generate(8000, 100, 3000, p_min=0.01, p_max=0.15, seed=18)
