@@ -47,7 +47,7 @@ METRIC = "alignments/sec"
 # seed, committed ncu summary of the dominant kernel
 THROUGHPUT = {
     "short": (1_000_000, 100_000, 150, 0.05, 2, "tier0_short_reads.txt"),
-    "long": (200_000, 20_000, 1000, 0.10, 3, "long_reads.txt"),
+    "long": (200_000, 20_000, 1000, 0.10, 3, "tier2_long_reads.txt"),
 }
 
 
@@ -83,8 +83,53 @@ def parse():
                     help="profiling case: run the --profile-kernel kernels twice over ONE batch of this "
                          "many pairs of the workload (a warm-up, then the launch to capture), and exit")
     ap.add_argument("--profile-kernel", choices=["tier", "aux"], default="tier")
+    ap.add_argument("--link", action="store_true",
+                    help="measure the CPU-GPU link: DMA copies between pinned host memory and HBM, and exit")
     ap.add_argument("--profile-first-tier", type=int, default=-1)
     return ap.parse_args()
+
+
+def run_link() -> int:
+    """Bandwidth of the CPU-GPU link (NVLink-C2C on GB300): DMA copies of
+    32 MiB - 1 GiB between pinned host memory and HBM, each direction alone
+    (best of 5, CUDA events) and both at once."""
+    import torch
+    torch.cuda.set_device(0)
+    res = {}
+    for mb in (32, 256, 1024):
+        n = mb << 20
+        h = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+        h.fill_(1)
+        d = torch.empty(n, dtype=torch.uint8, device="cuda")
+        s = torch.cuda.Stream()
+        for direction in ("h2d", "d2h"):
+            best = 1e9
+            for _ in range(5):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(s)
+                with torch.cuda.stream(s):
+                    if direction == "h2d":
+                        d.copy_(h, non_blocking=True)
+                    else:
+                        h.copy_(d, non_blocking=True)
+                e1.record(s)
+                torch.cuda.synchronize()
+                best = min(best, e0.elapsed_time(e1))
+            res[f"{direction}_{mb}MiB_GBs"] = round(n / best / 1e6, 1)
+    n = 256 << 20
+    h1, h2 = (torch.empty(n, dtype=torch.uint8, pin_memory=True) for _ in range(2))
+    d1, d2 = (torch.empty(n, dtype=torch.uint8, device="cuda") for _ in range(2))
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(s1):
+        d1.copy_(h1, non_blocking=True)
+    with torch.cuda.stream(s2):
+        h2.copy_(d2, non_blocking=True)
+    torch.cuda.synchronize()
+    res["both_directions_256MiB_each_GBs"] = round(2 * n / (time.perf_counter() - t0) / 1e9, 1)
+    print(json.dumps({"link": res}))
+    return 0
 
 
 def histories_from_cigars(cg: np.ndarray) -> np.ndarray:
@@ -549,6 +594,8 @@ def run_reference(args):
 
 def main():
     args = parse()
+    if args.link:
+        return run_link()
     if args.workload == "mixed":
         return run_mixed(args)
     if args.workload == "serve":
