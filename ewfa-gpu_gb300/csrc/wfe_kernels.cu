@@ -103,7 +103,29 @@ struct Tier {
     static constexpr int GPW = 32 / G;
     using OE = OpEntry<G>;
     using E = typename OE::T;
-    static constexpr size_t ops_bytes = round16(sizeof(E) * (size_t)DCAP * NC);
+    /* Row d of the backtrace store.  The 32-lane tiers keep only the chunks
+     * that score step d touches -- the contiguous range whose diagonals meet
+     * [-d, d] -- row after row (a triangle, 55-68 % of DCAP x NC entries):
+     * their store in shared memory is what limits their occupancy.  Tier 0
+     * keeps full rows: its occupancy is set by registers, and it is
+     * issue-bound, so it saves the index arithmetic instead. */
+    static constexpr bool TRI = G == 32;
+    static __host__ __device__ constexpr int chunk_lo(int d)
+    {
+        return !TRI ? 0 : (J - (d - 1 + G / 2) / G < 0 ? 0 : J - (d - 1 + G / 2) / G);
+    }
+    static __host__ __device__ constexpr int chunk_hi(int d)
+    {
+        return !TRI ? 2 * J : (J + (d + G / 2) / G > 2 * J ? 2 * J : J + (d + G / 2) / G);
+    }
+    static __host__ __device__ constexpr int row_entries(int d) { return chunk_hi(d) - chunk_lo(d) + 1; }
+    static constexpr int store_entries()
+    {
+        int t = 0;
+        for (int d = 1; d <= DCAP; ++d) t += row_entries(d);
+        return t;
+    }
+    static constexpr size_t ops_bytes = round16(sizeof(E) * (size_t)store_entries());
     static constexpr size_t chain_bytes = round16((size_t)DCAP + 1);
     static constexpr size_t runs_bytes = round16(sizeof(int) * ((size_t)DCAP + 1));
 };
@@ -332,14 +354,16 @@ __device__ __forceinline__ void tier_body(const AlignLaunch& A, uint32_t seq_wor
             const bool hit = state == ST_RUN && g == G / 2 && kt == 0 && O[J] == tlen;
             if (__ballot_sync(kFull, hit) & gmask) state = ST_DONE;
         }
-        for (int d = 1;; ++d) {
+        int rowbase = 0;  /* first store entry of step d's row (the same for every group) */
+        int rowD = 0;     /* ... of step D's row */
+        for (int d = 1;; rowbase += T::row_entries(d), ++d) {
             const bool run = state == ST_RUN;
             if (!__any_sync(kFull, run)) break;
             if (d > DCAP || (A.max_distance > 0 && d > A.max_distance)) {
                 if (run) state = (A.max_distance > 0 && d > A.max_distance) ? ST_OVERMAX : ST_OVERFLOW;
                 break;
             }
-            const int rowbase = (d - 1) * NC;
+            const int clo = T::chunk_lo(d);
             int N[NC];
             /* compute (src/kernels.cu:129-152) */
 #pragma unroll
@@ -358,7 +382,7 @@ __device__ __forceinline__ void tier_body(const AlignLaunch& A, uint32_t seq_wor
                     const unsigned blo = __ballot_sync(kFull, m & 1);
                     const unsigned bhi = __ballot_sync(kFull, m & 2);
                     if (!PREDICT && run && g == 0)
-                        OE::put(ops, rowbase + c, (blo >> ((grp * G) & 31)) & gbits,
+                        OE::put(ops, rowbase + c - clo, (blo >> ((grp * G) & 31)) & gbits,
                                 (bhi >> ((grp * G) & 31)) & gbits);
                     const int k = lo_k + g;
                     N[c] = (run && k >= -d && k <= d) ? (m >> 2) : -1;
@@ -381,6 +405,7 @@ __device__ __forceinline__ void tier_body(const AlignLaunch& A, uint32_t seq_wor
             if ((__ballot_sync(kFull, hit) & gmask) && run) {
                 state = ST_DONE;
                 D = d;
+                rowD = rowbase;
             }
         }
 
@@ -395,12 +420,14 @@ __device__ __forceinline__ void tier_body(const AlignLaunch& A, uint32_t seq_wor
             int walk_ok = 1;
             if (g == 0) {
                 int k = kt;
+                int row = rowD;
                 for (int s = D; s >= 1; --s) {
                     if (k < -s || k > s) { walk_ok = 0; break; }
                     const int idx = k + G / 2 + G * J;
-                    const int op = OE::get(ops, (s - 1) * NC + idx / G, idx & (G - 1));
+                    const int op = OE::get(ops, row + idx / G - T::chunk_lo(s), idx & (G - 1));
                     chain[s - 1] = (uint8_t)op;
                     k += op - 2;
+                    if (s > 1) row -= T::row_entries(s - 1);
                 }
                 if (k != 0) walk_ok = 0;
             }
