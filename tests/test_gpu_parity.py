@@ -411,6 +411,31 @@ def test_long_tiers_without_distance_limit():
     compare_with_oracle(ascii, pairs, 12000, dist, cg, st)
 
 
+@pytest.mark.parametrize("first_tier", [5, 6])
+def test_cta_tiers_first_with_and_without_cap(first_tier):
+    """The CTA-per-pair tiers as the first tier of every pair: identical
+    pairs (distance 0), empty and one-base sequences, short and long pairs,
+    with no cap and with a distance cap that stops some of them."""
+    torch_cuda()
+    rng = np.random.default_rng(41)
+    ascii, pairs = wfe.generate(1500, 50, 2500, p_min=0.0, p_max=0.12, seed=41)
+    seqs = [(ascii[q["p_off"]:q["p_off"] + q["p_len"]].tobytes(), ascii[q["t_off"]:q["t_off"] + q["t_len"]].tobytes())
+            for q in pairs]
+    t = np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, 700)].tobytes()
+    seqs += [(t, t), (b"", b""), (b"", b"ACGT"), (b"ACGT", b""), (b"A", b"C"), (b"A", b"A"), (t[:40], t)]
+    ascii, pairs = wfe.pairs_from_list(seqs)
+    for cap in (0, 100):
+        with wfe.Context(max_seq_len=3000, cigar_stride=4096, max_distance=cap, batch_size=700) as ctx:
+            ctx.set_policy([3000], [first_tier])
+            dist, cg, st = ctx.align(ascii, pairs)
+            assert ctx.stats()["tier_launches"][first_tier] > 0
+        if cap:
+            assert (st == wfe.PAIR_OVER_MAX_DISTANCE).any() and (st == wfe.PAIR_OK).any()
+        else:
+            assert (st == wfe.PAIR_OK).all()
+        compare_with_oracle(ascii, pairs, 4096, dist, cg, st, max_distance=cap)
+
+
 def test_length_buckets_same_results():
     """Mixed lengths sorted into length buckets, each with its own first tier
     and launch shapes: every result equals the oracle's and the one-bucket
