@@ -417,6 +417,11 @@ def dist_env():
     return world, rank, local
 
 
+def shard_seed(rank: int) -> int:
+    """Seed of one rank's shard: every rank aligns its own pairs (weak scaling)."""
+    return SEED + 1000 * rank
+
+
 def reduce_max(x: float, world: int, device=None) -> float:
     """Max of x over ranks (identity for one process)."""
     if world <= 1:
@@ -616,7 +621,7 @@ def main():
         dist.init_process_group("nccl", device_id=device)
 
     # this rank's shard of the workload
-    ascii, pairs = wfe.generate(PAIRS, LENGTH, p_min=EDIT_P, seed=SEED + 1000 * rank)
+    ascii, pairs = wfe.generate(PAIRS, LENGTH, p_min=EDIT_P, seed=shard_seed(rank))
     nb = PAIRS // BATCH
     stream = torch.cuda.Stream(device=device)
 
