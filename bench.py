@@ -254,7 +254,8 @@ def run_mixed(args) -> int:
             st = ctx.stats()
             res[mode] = {"seconds": ms / 1e3, "alignments_per_s": n / (ms / 1e3), "first_tiers": tiers,
                          "tune_seconds": round(t_tune, 3), "kernel_launches": st["kernel_launches"],
-                         "tier_launches": st["tier_launches"][:7], "tier_passed": st["tier_passed"][:7]}
+                         "tier_launches": st["tier_launches"][:7], "tier_passed": st["tier_passed"][:7],
+                         "chain_ms_by_first_tier": [round(x, 2) for x in st["tier_ms"][:7]]}
         outs[mode] = (d_dist.cpu().numpy(), d_st.cpu().numpy(), d_cg)
     same_dist = all(np.array_equal(outs["plain"][0], outs[m][0]) for m in modes)
     same_status = all(np.array_equal(outs["plain"][1], outs[m][1]) for m in modes)
