@@ -499,17 +499,22 @@ def measured_hbm_peak():
         return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes per launch of the dominant kernel from the committed ncu
-    summary, if one records it (a line 'traffic_bytes_per_launch: N')."""
+def profiled(key: str):
+    """A figure of the dominant kernel's committed ncu summary (a line
+    'key: N'), or None."""
     p = os.path.join(ROOT, "profiles", PROFILE)
     try:
         for line in open(p):
-            if line.startswith("traffic_bytes_per_launch:"):
+            if line.startswith(key + ":"):
                 return float(line.split(":", 1)[1])
     except OSError:
         pass
     return None
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the dominant kernel (ncu, scaled to one launch)."""
+    return profiled("traffic_bytes_per_launch")
 
 
 def cigar_lengths(cg: np.ndarray) -> np.ndarray:
@@ -744,6 +749,10 @@ def main():
                        "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "integer_pipes": {"alu_pipe_pct_of_peak": profiled("alu_pipe_pct_of_peak"),
+                                           "issue_slots_busy_pct": profiled("issue_slots_busy_pct"),
+                                           "source": "ncu, profiles/" + PROFILE,
+                                           "note": "the kernel is bound by its integer pipes, not by HBM"},
                          "kernel": f"tier_kernel tier {top}" + (" and the tiers it hands pairs on to (one timed "
                                                                      "chain)" if any(st["tier_passed"]) else ""),
                          "alg_bytes_per_launch": alg_bytes,
