@@ -37,6 +37,10 @@
 namespace {
 
 struct Option {
+    Option(const char* n, const char* d, char s, const char* l, bool r, int k)
+        : name(n), description(d), short_arg(s), long_arg(l), required(r), kind(k)
+    {
+    }
     const char* name;
     const char* description;
     char short_arg;

@@ -120,7 +120,11 @@ typedef struct wfe_stats {
 
 /* Create a context on cfg->device: streams, device buffers for one batch in
  * each pipeline stage, pinned staging.  Replaces the Sequences constructor
- * and GPU_memory_init (src/wavefront.cuh:458-485, src/wavefront.cu:29-108). */
+ * and GPU_memory_init (src/wavefront.cuh:458-485, src/wavefront.cu:29-108).
+ * Threading: a context is used by one thread at a time; different contexts
+ * may be used from different threads at once.  Every call on a context makes
+ * its device the calling thread's current device (as the reference's
+ * cudaSetDevice does, src/aligner.cu:147). */
 int wfe_create(const wfe_config* cfg, wfe_ctx** out);
 
 /* Release everything the context owns.  Replaces GPU_memory_free
@@ -351,7 +355,9 @@ typedef struct wfe_server_stats {
  * less free memory than the arena asks for. */
 int wfe_server_create(const wfe_server_config* cfg, wfe_server** out);
 
-/* Finish every submitted request, then release everything. */
+/* Finish every submitted request, then release everything.  No other call
+ * on the server (a wfe_poll waiting in another thread included) may be in
+ * progress or follow. */
 void wfe_server_destroy(wfe_server* srv);
 
 /* Queue n pairs of ascii (ascii_bytes long; descriptors as in wfe_align) for
