@@ -94,6 +94,10 @@ namespace {
 int fail_cuda(wfe_ctx* ctx, cudaError_t e)
 {
     if (ctx) ctx->last_cuda_error = (int)e;
+    /* the error is reported here: clear the runtime's record of it (a failed
+     * allocation is not sticky), so that a later cudaGetLastError -- ours or
+     * the caller's -- does not report it again */
+    cudaGetLastError();
     return e == cudaErrorMemoryAllocation ? WFE_ERR_OUT_OF_MEMORY : WFE_ERR_CUDA;
 }
 
@@ -369,6 +373,7 @@ int create_context(const wfe_config* cfg, uint64_t budget5, uint64_t budget6, wf
 
     auto bail = [&](cudaError_t err) {
         g_last_create_error = (int)err;
+        cudaGetLastError(); /* reported here, not to a later call */
         for (auto& s : ctx->st) free_stage(s);
         cudaFree(ctx->d_ops_scratch);
         cudaFree(ctx->d_passed);

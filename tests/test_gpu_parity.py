@@ -494,3 +494,39 @@ def test_autotune_installs_and_caches(tmp_path):
         assert ctx3.policy()[2] is False
     assert open(cache).read().count("first_tier") == 2
     compare_with_oracle(ascii, pairs, 2048, *got)
+
+
+def test_exhaustive_tiny_pairs():
+    """Every pair of sequences over ACGT of length 0-4 (341 x 341 pairs), and
+    a sample of lengths 5-6: the small cases where sentinels, the first and
+    last diagonals and empty sequences meet."""
+    torch_cuda()
+    import itertools
+    seqs = [b""]
+    for L in range(1, 5):
+        seqs += [bytes(t) for t in itertools.product(b"ACGT", repeat=L)]
+    pairs = [(p, t) for p in seqs for t in seqs]
+    rng = np.random.default_rng(3)
+    for _ in range(20000):
+        lp, lt = int(rng.integers(5, 7)), int(rng.integers(0, 7))
+        pairs.append((np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, lp)].tobytes(),
+                      np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, lt)].tobytes()))
+    ascii, desc = wfe.pairs_from_list(pairs)
+    with wfe.Context(max_seq_len=8, cigar_stride=16, batch_size=50000) as ctx:
+        dist, cg, st = ctx.align(ascii, desc)
+    assert (st == wfe.PAIR_OK).all()
+    compare_with_oracle(ascii, desc, 16, dist, cg, st)
+
+
+def test_allocation_failure_is_reported_and_leaves_the_device_usable():
+    """A context whose buffers cannot be allocated fails with
+    WFE_ERR_OUT_OF_MEMORY; nothing is left half-made and the next context
+    works."""
+    torch_cuda()
+    with pytest.raises(wfe.WfeError) as e:
+        wfe.Context(max_seq_len=2000, batch_size=200_000_000)  # 800 GB of ASCII staging per stage
+    assert e.value.code == wfe.ERR_OUT_OF_MEMORY
+    ascii, pairs = wfe.generate(2000, 150, p_min=0.05, seed=9)
+    with wfe.Context(max_seq_len=300, cigar_stride=152) as ctx:
+        dist, cg, st = ctx.align(ascii, pairs)
+    compare_with_oracle(ascii, pairs, 152, dist, cg, st)
