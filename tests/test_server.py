@@ -153,3 +153,16 @@ def test_memory_admission_limits_batches(pool):
     with pytest.raises(wfe.WfeError) as e:
         wfe.Server(max_seq_len=MAX_LEN, memory_bytes=1024)  # not one pair fits
     assert e.value.code == wfe.ERR_INVALID_ARGUMENT
+
+
+def test_admission_refused_when_the_arena_does_not_fit(pool):
+    """A server whose arena is larger than the free device memory is refused
+    (WFE_ERR_BUSY) and the device stays usable."""
+    ascii, pairs = pool
+    with pytest.raises(wfe.WfeError) as e:
+        wfe.Server(max_seq_len=MAX_LEN, memory_bytes=1 << 50)
+    assert e.value.code == wfe.ERR_BUSY
+    with wfe.Server(max_seq_len=MAX_LEN, lanes=1) as srv:
+        r = srv.submit(ascii, pairs[:200])
+        assert srv.poll(r)
+    check_same(r, alone(ascii, pairs[:200]))
