@@ -517,6 +517,37 @@ def profiled_traffic():
     return profiled("traffic_bytes_per_launch")
 
 
+def pageable_e2e(ascii, pairs, reps, local, world, device, want_dist) -> dict:
+    """wfe_align with ordinary (pageable) numpy arrays, as most callers hold
+    them: the inputs as generated and fresh np.empty outputs allocated inside
+    the timed region every step.  Staged (cudaMemcpyAsync through the
+    driver's bounce buffers) and in place through the CPU's page tables
+    (WFE_FLAG_PAGEABLE_IN_PLACE: the library makes the fresh output pages
+    present on the host, batch by batch, ahead of the kernels)."""
+    import torch
+    out = {"unit": "alignments/s", "outputs": "fresh np.empty arrays every step"}
+    for name, flags in (("staged", 0), ("in_place", wfe.FLAG_PAGEABLE_IN_PLACE)):
+        ctx = wfe.Context(max_seq_len=MAX_SEQ_LEN, batch_size=BATCH, cigar_stride=CIGAR_STRIDE, device=local,
+                          flags=flags)
+        ctx.align(ascii, pairs)  # warm-up
+        ctx.reset_stats()
+        barrier(world, device)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            res = (np.empty(PAIRS, np.int32), np.empty((PAIRS, CIGAR_STRIDE), np.int8), np.empty(PAIRS, np.uint8))
+            ctx.align(ascii, pairs, out=res)
+        torch.cuda.synchronize()
+        dt = reduce_max(time.perf_counter() - t0, world, device)
+        st = ctx.stats()
+        ctx.close()
+        if not np.array_equal(res[0], want_dist):
+            raise SystemExit(f"pageable ({name}) and pinned results differ")
+        out[name] = world * reps * PAIRS / dt
+        out[name + "_mapped_batches"] = int(st["mapped_batches"])
+    return out
+
+
 def cigar_lengths(cg: np.ndarray) -> np.ndarray:
     """Bytes of each encoded CIGAR before its terminator."""
     z = cg == 0
@@ -729,6 +760,7 @@ def main():
                         "over NVLink-C2C" if in_place else "staged cudaMemcpyAsync copies")}
     if not (np.array_equal(h_dist, d_dist.cpu().numpy())):
         raise SystemExit("host-buffer and device-buffer results differ")
+    e2e["pageable"] = pageable_e2e(ascii, pairs, reps, local, world, device, h_dist)
 
     base = None
     ref_cuda = None

@@ -28,6 +28,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <ctime>
+#include <memory>
 #include <string>
 #include <thread>
 #include <vector>
@@ -104,9 +105,11 @@ double now_s()
 
 struct Share {
     size_t first = 0, n = 0;
-    std::vector<int32_t> dist;
-    std::vector<int8_t> cigar;
-    std::vector<uint8_t> status;
+    /* left uninitialised: libwfe makes the pages present (in parallel)
+     * and the kernels write them in place */
+    std::unique_ptr<int32_t[]> dist;
+    std::unique_ptr<int8_t[]> cigar;
+    std::unique_ptr<uint8_t[]> status;
     int rc = WFE_OK;
     std::string what;
 };
@@ -218,25 +221,26 @@ int main(int argc, char** argv)
         cfg.batch_size = (uint32_t)b;
         cfg.max_distance = (int32_t)max_distance;
         cfg.cigar_stride = stride;
+        cfg.flags = WFE_FLAG_PAGEABLE_IN_PLACE; /* the results go straight to this share's arrays */
         wfe_ctx* ctx = nullptr;
         sh.rc = wfe_create(&cfg, &ctx);
         if (sh.rc != WFE_OK) {
             sh.what = "wfe_create";
             return;
         }
-        sh.dist.resize(sh.n);
-        sh.cigar.resize(sh.n * stride);
-        sh.status.resize(sh.n);
+        sh.dist.reset(new int32_t[sh.n]);
+        sh.cigar.reset(new int8_t[sh.n * stride]);
+        sh.status.reset(new uint8_t[sh.n]);
         /* the pairs of this share: in the file's pinned descriptors, or the
          * empty tail */
         if (sh.first + sh.n <= pf.n) {
-            sh.rc = wfe_align(ctx, pf.ascii, pf.ascii_bytes, pf.pairs + sh.first, sh.n, sh.dist.data(), sh.cigar.data(),
-                              sh.status.data());
+            sh.rc = wfe_align(ctx, pf.ascii, pf.ascii_bytes, pf.pairs + sh.first, sh.n, sh.dist.get(), sh.cigar.get(),
+                              sh.status.get());
         } else {
             std::vector<wfe_pair> mine(sh.n);
             for (size_t i = 0; i < sh.n; ++i) mine[i] = *pair_at(sh.first + i);
-            sh.rc = wfe_align(ctx, pf.ascii, pf.ascii_bytes, mine.data(), sh.n, sh.dist.data(), sh.cigar.data(),
-                              sh.status.data());
+            sh.rc = wfe_align(ctx, pf.ascii, pf.ascii_bytes, mine.data(), sh.n, sh.dist.get(), sh.cigar.get(),
+                              sh.status.get());
         }
         if (sh.rc != WFE_OK) sh.what = "wfe_align";
         wfe_destroy(ctx);

@@ -11,14 +11,20 @@
  * synchronisation between kernels.
  */
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <fstream>
 #include <sstream>
 #include <string>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <new>
+#include <thread>
 #include <vector>
+
+#include <sys/mman.h>
+#include <unistd.h>
 
 #include "wfe.h"
 #include "wfe_internal.h"
@@ -68,6 +74,7 @@ struct BucketPlan {
 struct wfe_ctx {
     wfe_config cfg{};
     int sm_count = 0;
+    bool host_page_tables = false;             /* the device reads pageable memory through the CPU's page tables */
     int nbuckets = 1;
     BucketPlan bucket[kMaxBuckets];
     bool predict = false;                      /* route pairs by predicted distance */
@@ -385,6 +392,10 @@ int create_context(const wfe_config* cfg, uint64_t budget5, uint64_t budget6, wf
 
     e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, c.device);
     if (e != cudaSuccess) return bail(e);
+    int hpt = 0;
+    e = cudaDeviceGetAttribute(&hpt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, c.device);
+    if (e != cudaSuccess) return bail(e);
+    ctx->host_page_tables = hpt != 0;
     /* Global scratch is sized for the longest sequences (max_seq_len); a
      * bucket of shorter sequences has more resident CTAs and uses at most
      * the CTAs that scratch was sized for. */
@@ -594,9 +605,70 @@ struct HostJob {
     const uint32_t* t_len;
 };
 
-/* Device address of a pinned, device-mapped host buffer (NULL when p is
- * pageable or not host memory). */
-void* mapped_address(const void* p)
+/* A pageable host range that the device reaches through the CPU's page
+ * tables.  Its pages are made present on the host before the device touches
+ * them: a page the device finds missing is filled by a fault that costs ~5x
+ * the host's own first touch (152 MB of fresh output: 33 ms from the GPU,
+ * 6.4 ms from one host thread, 1.3 ms from eight).  One byte per page is
+ * touched.  Input pages are read.  Output pages that were missing get a 0
+ * written (no read first: a read maps the shared zero page, and the write
+ * after it costs a copy-on-write fault, 40x slower); present ones are read
+ * and written back, which also shows that they are writable.  Every byte
+ * touched lies inside the sub-range being touched, so touching one batch's
+ * outputs never writes bytes of a batch the device is already writing. */
+struct HostRange {
+    char* p = nullptr;
+    size_t bytes = 0;
+    bool write = false;
+    uintptr_t lo = 0;                    /* first page */
+    std::vector<unsigned char> resident; /* per page, when the call started */
+    size_t missing = 0;                  /* pages not present then */
+
+    static size_t page()
+    {
+        static const size_t pg = (size_t)sysconf(_SC_PAGESIZE);
+        return pg;
+    }
+
+    /* false when part of the range is not mapped at all (mincore fails) */
+    bool map(const void* q, size_t n, bool w)
+    {
+        p = (char*)q;
+        bytes = n;
+        write = w;
+        lo = (uintptr_t)q & ~(uintptr_t)(page() - 1);
+        const uintptr_t hi = (uintptr_t)q + n;
+        resident.assign((hi - lo + page() - 1) / page(), 0);
+        if (mincore((void*)lo, hi - lo, resident.data()) != 0) return false;
+        missing = 0;
+        for (unsigned char r : resident) missing += (r & 1u) ? 0u : 1u;
+        return true;
+    }
+
+    /* touch the pages that overlap bytes [off0, off1) of the range */
+    void touch(size_t off0, size_t off1) const
+    {
+        if (off0 >= off1) return;
+        const uintptr_t a0 = (uintptr_t)p + off0, a1 = (uintptr_t)p + off1;
+        for (size_t k = (a0 - lo) / page(); k <= (a1 - 1 - lo) / page(); ++k) {
+            volatile char* q = (volatile char*)std::max<uintptr_t>(a0, lo + k * page());
+            if (write && !(resident[k] & 1u)) {
+                *q = 0;
+            } else {
+                const char v = *q;
+                if (write) *q = v;
+            }
+        }
+    }
+};
+
+/* Device address of a host buffer that the kernels can use in place, or
+ * NULL when it has to be staged.  Pinned, device-mapped memory is always
+ * used in place.  Pageable memory is used in place when `pageable` (the
+ * caller's WFE_FLAG_PAGEABLE_IN_PLACE on a device that reads the CPU's page
+ * tables) and all of it is mapped; an input's missing pages are read here,
+ * an output's are left to the caller (range filled in). */
+void* mapped_address(const void* p, size_t bytes, bool write, bool pageable, HostRange* range)
 {
     if (!p) return nullptr;
     cudaPointerAttributes at{};
@@ -604,8 +676,78 @@ void* mapped_address(const void* p)
         cudaGetLastError(); /* pageable memory of an older driver: not mapped */
         return nullptr;
     }
-    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+    if (at.type == cudaMemoryTypeHost) return at.devicePointer;
+    if (at.type != cudaMemoryTypeUnregistered || !pageable || bytes == 0) return nullptr;
+    HostRange r;
+    if (!r.map(p, bytes, write)) return nullptr;
+    if (write) {
+        *range = std::move(r);
+    } else if (r.missing) {
+        r.touch(0, bytes);
+    }
+    return const_cast<void*>(p);
 }
+
+/* The output pages of a call's batches, touched in batch order by helper
+ * threads while the device aligns the earlier batches; the host launches
+ * batch b once its pages are done.  Threads are used only when more than
+ * 8 MB of output pages are missing; otherwise ready() touches the batch
+ * itself. */
+class OutputPages {
+public:
+    OutputPages(std::vector<HostRange> ranges, std::vector<size_t> unit, size_t batch, size_t n)
+        : r_(std::move(ranges)), unit_(std::move(unit)), batch_(batch), n_(n)
+    {
+        size_t missing = 0;
+        for (const HostRange& r : r_) missing += r.missing;
+        nb_ = batch_ ? (n_ + batch_ - 1) / batch_ : 0;
+        if (r_.empty() || missing * HostRange::page() < (8u << 20) || nb_ == 0) return;
+        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+        nthreads_ = std::min(8u, hw);
+        left_.reset(new std::atomic<unsigned>[nb_]);
+        for (size_t b = 0; b < nb_; ++b) left_[b].store(nthreads_);
+        for (unsigned t = 0; t < nthreads_; ++t) th_.emplace_back([this, t] { run(t); });
+    }
+    ~OutputPages()
+    {
+        stop_.store(true);
+        for (auto& x : th_) x.join();
+    }
+    /* batch b's output pages are present */
+    void ready(size_t b)
+    {
+        if (r_.empty() || b >= nb_) return;
+        if (th_.empty()) {
+            stripe(b, 0, 1);
+            return;
+        }
+        while (left_[b].load(std::memory_order_acquire) != 0) std::this_thread::yield();
+    }
+
+private:
+    void stripe(size_t b, unsigned t, unsigned T) const
+    {
+        const size_t i0 = b * batch_, i1 = std::min(n_, i0 + batch_);
+        for (size_t k = 0; k < r_.size(); ++k) {
+            const size_t o0 = i0 * unit_[k], o1 = i1 * unit_[k];
+            r_[k].touch(o0 + (o1 - o0) * t / T, o0 + (o1 - o0) * (t + 1) / T);
+        }
+    }
+    void run(unsigned t)
+    {
+        for (size_t b = 0; b < nb_ && !stop_.load(std::memory_order_relaxed); ++b) {
+            stripe(b, t, nthreads_);
+            left_[b].fetch_sub(1, std::memory_order_release);
+        }
+    }
+    std::vector<HostRange> r_;
+    std::vector<size_t> unit_; /* bytes per pair in each range */
+    size_t batch_, n_, nb_ = 0;
+    unsigned nthreads_ = 0;
+    std::unique_ptr<std::atomic<unsigned>[]> left_;
+    std::atomic<bool> stop_{false};
+    std::vector<std::thread> th_;
+};
 
 int align_host(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, int8_t* cigar_out,
                uint8_t* status_out)
@@ -615,15 +757,22 @@ int align_host(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, in
     WFE_CUDA(ctx, cudaSetDevice(c.device));
     const bool want_cigar = cigar_out && c.cigar_stride;
 
-    /* pinned inputs are read in place, pinned outputs written in place */
-    const char* m_ascii = (const char*)mapped_address(job.ascii);
-    const wfe_pair* m_pairs = job.pairs ? (const wfe_pair*)mapped_address(job.pairs) : nullptr;
-    const uint32_t* m_plen = job.pairs ? nullptr : (const uint32_t*)mapped_address(job.p_len);
-    const uint32_t* m_tlen = job.pairs ? nullptr : (const uint32_t*)mapped_address(job.t_len);
+    /* pinned inputs are read in place, pinned outputs written in place, and
+     * so are pageable ones when asked for on a device that can */
+    const bool pg = (c.flags & WFE_FLAG_PAGEABLE_IN_PLACE) && ctx->host_page_tables && n > 0;
+    HostRange r_dist, r_cigar, r_status, unused;
+    const char* m_ascii = (const char*)mapped_address(job.ascii, job.ascii_bytes, false, pg, &unused);
+    const wfe_pair* m_pairs =
+        job.pairs ? (const wfe_pair*)mapped_address(job.pairs, n * sizeof(wfe_pair), false, pg, &unused) : nullptr;
+    const uint32_t* m_plen =
+        job.pairs ? nullptr : (const uint32_t*)mapped_address(job.p_len, n * 4u, false, pg, &unused);
+    const uint32_t* m_tlen =
+        job.pairs ? nullptr : (const uint32_t*)mapped_address(job.t_len, n * 4u, false, pg, &unused);
     const bool in_place = m_ascii && job.ascii_bytes > 0 && (job.pairs ? m_pairs != nullptr : (m_plen && m_tlen));
-    int32_t* m_dist = (int32_t*)mapped_address(dist_out);
-    int8_t* m_cigar = want_cigar ? (int8_t*)mapped_address(cigar_out) : nullptr;
-    uint8_t* m_status = status_out ? (uint8_t*)mapped_address(status_out) : nullptr;
+    int32_t* m_dist = (int32_t*)mapped_address(dist_out, n * 4u, true, pg, &r_dist);
+    int8_t* m_cigar =
+        want_cigar ? (int8_t*)mapped_address(cigar_out, n * (size_t)c.cigar_stride, true, pg, &r_cigar) : nullptr;
+    uint8_t* m_status = status_out ? (uint8_t*)mapped_address(status_out, n, true, pg, &r_status) : nullptr;
     const bool out_in_place = m_dist && (!want_cigar || m_cigar) && (!status_out || m_status);
 
     size_t B = c.batch_size;
@@ -633,6 +782,16 @@ int align_host(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, in
         if (fit == 0) return WFE_ERR_SEQ_TOO_LONG;
         B = std::min(B, fit);
     }
+    /* pageable outputs written in place: their pages are made present batch
+     * by batch, ahead of the device */
+    std::vector<HostRange> pages;
+    std::vector<size_t> unit;
+    if (out_in_place) {
+        if (r_dist.p) pages.push_back(std::move(r_dist)), unit.push_back(4u);
+        if (r_cigar.p) pages.push_back(std::move(r_cigar)), unit.push_back(c.cigar_stride);
+        if (r_status.p) pages.push_back(std::move(r_status)), unit.push_back(1u);
+    }
+    OutputPages out_pages(std::move(pages), std::move(unit), B, n);
     const int nstages = (c.flags & WFE_FLAG_NO_PIPELINE) ? 1 : kStages;
     size_t bi = 0;
     size_t nb = 0;
@@ -718,6 +877,7 @@ int align_host(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, in
             L.stride = job.stride;
         }
         if (out_in_place) {
+            out_pages.ready(bi);
             const int r = run_chain(ctx, st, L, (uint32_t)nb, m_dist + b0,
                                     want_cigar ? m_cigar + b0 * c.cigar_stride : nullptr,
                                     status_out ? m_status + b0 : nullptr, s);

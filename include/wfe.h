@@ -96,6 +96,11 @@ typedef struct wfe_config {
 #define WFE_FLAG_DEVICE_ONLY 4u   /* no staging buffers for host calls: the context
                                      serves wfe_align_device only (wfe_align and
                                      wfe_align_strided return WFE_ERR_INVALID_ARGUMENT) */
+#define WFE_FLAG_PAGEABLE_IN_PLACE 8u /* host calls on a device that reads pageable
+                                     memory through the CPU's page tables (ATS over
+                                     NVLink-C2C on GB300): pageable buffers are used
+                                     in place like pinned ones (see wfe_align);
+                                     ignored on other devices */
 
 typedef struct wfe_ctx wfe_ctx;
 
@@ -112,8 +117,9 @@ typedef struct wfe_stats {
     uint64_t tier_launches[8]; /* launches of each tier's kernel */
     double tier_ms[8];         /* GPU milliseconds of the chains started at each
                                   tier (only with WFE_FLAG_KERNEL_TIMING) */
-    uint64_t mapped_batches;   /* host-call batches whose pinned inputs the
-                                  kernels read in place */
+    uint64_t mapped_batches;   /* host-call batches whose inputs the kernels
+                                  read in place (pinned, or pageable with
+                                  WFE_FLAG_PAGEABLE_IN_PLACE) */
 } wfe_stats;
 
 /* ---- lifecycle -------------------------------------------------------- */
@@ -207,7 +213,11 @@ int wfe_autotune(wfe_ctx* ctx, const char* d_ascii, const wfe_pair* d_pairs, siz
  * descriptors are copied in (the call then returns WFE_ERR_SEQ_TOO_LONG or
  * WFE_ERR_INVALID_ARGUMENT for bad pairs before aligning anything), results
  * copied out, with the copies of one batch overlapping the kernels of the
- * other. */
+ * other.  With WFE_FLAG_PAGEABLE_IN_PLACE on a device that reads the CPU's
+ * page tables, pageable buffers are used in place as pinned ones are (bad
+ * pairs reported per pair); every page is touched on the host first, by up
+ * to eight threads, so that none is first faulted in by the GPU.  A range
+ * that is not wholly mapped is staged. */
 int wfe_align(wfe_ctx* ctx, const char* ascii, size_t ascii_bytes,
               const wfe_pair* pairs, size_t n, int32_t* dist_out,
               int8_t* cigar_out, uint8_t* status_out);

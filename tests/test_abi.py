@@ -138,3 +138,24 @@ def test_struct_layouts_match_the_header(tmp_path):
         want.append(C.sizeof(cls))
         want += [getattr(cls, f).offset for f in fields]
     assert got == want
+
+
+def test_constants_match_the_header():
+    """Every WFE_ status, pair status, flag and limit of include/wfe.h has the
+    same value in the Python mirror."""
+    txt = open(os.path.join(ROOT, "include", "wfe.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    found = {}
+    for name, val in re.findall(r"#define\s+WFE_([A-Z0-9_]+)\s+(\(?[0-9]+u?(?:\s*<<\s*[0-9]+)?\)?)", txt):
+        found[name] = eval(val.replace("u", ""))
+    for name, val in re.findall(r"\bWFE_((?:ERR|PAIR)_[A-Z_]+|OK)\s*=\s*([0-9]+)", txt):
+        found[name] = int(val)
+    skip = {"H", "ABI_VERSION", "MAX_BUCKETS"}
+    checked = 0
+    for name, val in found.items():
+        if name in skip:
+            continue
+        assert hasattr(wfe, name), name
+        assert getattr(wfe, name) == val, name
+        checked += 1
+    assert checked >= 22 and found["FLAG_PAGEABLE_IN_PLACE"] == 8

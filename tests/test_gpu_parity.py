@@ -364,6 +364,60 @@ def test_pinned_bad_descriptors_flagged_per_pair():
     np.testing.assert_array_equal(d[ok], od)
 
 
+def test_pageable_buffers_in_place_with_the_flag():
+    """WFE_FLAG_PAGEABLE_IN_PLACE: plain (pageable) inputs and outputs,
+    including output arrays whose pages were never touched, are used in place
+    through the CPU's page tables.  Results equal the staged path's in both
+    layouts, and bad descriptors are flagged per pair as with pinned buffers."""
+    torch_cuda()
+    ascii, pairs = wfe.generate(60000, 150, p_min=0.05, seed=17)
+    n, stride = len(pairs), 152
+    with wfe.Context(max_seq_len=300, batch_size=7000, cigar_stride=stride) as ctx:
+        want = ctx.align(ascii, pairs)
+        assert ctx.stats()["mapped_batches"] == 0
+    flags = wfe.FLAG_PAGEABLE_IN_PLACE
+    with wfe.Context(max_seq_len=300, batch_size=7000, cigar_stride=stride, flags=flags) as ctx:
+        # fresh pages: 9 MB of CIGAR slots, made present by several host threads
+        out = (np.empty(n, np.int32), np.empty((n, stride), np.int8), np.empty(n, np.uint8))
+        got = ctx.align(ascii, pairs, out=out)
+        assert ctx.stats()["mapped_batches"] == 9
+        assert ctx.stats()["h2d_bytes"] == 0 and ctx.stats()["d2h_bytes"] == 0
+        np.testing.assert_array_equal(got[0], want[0])
+        np.testing.assert_array_equal(got[2], want[2])
+        assert_same_cigars(got[1], want[1])
+        # pinned outputs with pageable inputs, and the reverse
+        got = ctx.align(ascii, pairs, out=tuple(_pinned(o) for o in out))
+        np.testing.assert_array_equal(got[0], want[0])
+        assert_same_cigars(got[1], want[1])
+        got = ctx.align(_pinned(ascii), _pinned(pairs))
+        np.testing.assert_array_equal(got[0], want[0])
+        assert_same_cigars(got[1], want[1])
+
+        # strided layout
+        sub = pairs[:2000]
+        unp = 304
+        buf = np.zeros(2 * unp * len(sub), np.uint8)
+        for i, q in enumerate(sub):
+            buf[2 * i * unp: 2 * i * unp + q["p_len"]] = ascii[q["p_off"]: q["p_off"] + q["p_len"]]
+            buf[(2 * i + 1) * unp: (2 * i + 1) * unp + q["t_len"]] = ascii[q["t_off"]: q["t_off"] + q["t_len"]]
+        ctx.reset_stats()
+        gs = ctx.align_strided(buf, unp, sub["p_len"].copy(), sub["t_len"].copy())
+        assert ctx.stats()["mapped_batches"] == 1
+        np.testing.assert_array_equal(gs[0], want[0][:2000])
+        assert_same_cigars(gs[1], want[1][:2000])
+
+        # bad descriptors are flagged per pair, not refused
+        bad = pairs[:100].copy()
+        bad[3]["p_off"] = len(ascii) + 1000
+        bad[5]["t_len"] = len(ascii)
+        d, cg, st = ctx.align(ascii, bad)
+        assert st[3] == wfe.PAIR_OUT_OF_RANGE and st[5] == wfe.PAIR_OUT_OF_RANGE
+        ok = np.ones(100, bool)
+        ok[[3, 5]] = False
+        assert (st[ok] == wfe.PAIR_OK).all()
+        np.testing.assert_array_equal(d[ok], want[0][:100][ok])
+
+
 def test_pinned_strided_layout():
     torch_cuda()
     seqs = []
