@@ -562,11 +562,49 @@ def cpu_baseline(ascii, pairs, nthreads):
     import oracle
     oracle.build(ref=False)
     t0 = time.perf_counter()
-    oracle.align_batch(ascii, pairs["p_off"], pairs["p_len"], pairs["t_off"], pairs["t_len"], CIGAR_STRIDE,
-                       nthreads=nthreads)
+    _, _, _, (cells, words) = oracle.align_batch(ascii, pairs["p_off"], pairs["p_len"], pairs["t_off"],
+                                                 pairs["t_len"], CIGAR_STRIDE, nthreads=nthreads)
     dt = time.perf_counter() - t0
     return {"value": len(pairs) / dt, "unit": METRIC, "cores": nthreads, "kind": "port",
-            "sample": f"all {len(pairs):,} pairs of the workload, {nthreads} threads, {dt:.2f} s"}
+            "sample": f"all {len(pairs):,} pairs of the workload, {nthreads} threads, {dt:.2f} s",
+            "counts": {"cells": int(cells), "extend_words": int(words), "pairs": len(pairs)}}
+
+
+def int32_peak(device: int) -> dict | None:
+    """32-bit integer operations per second of the device, measured by
+    ewfa-gpu_gb300/csrc/int_peak.cu (three-input adds and logic ops, every SM
+    full; best of 5 launches)."""
+    import ctypes as C
+    path = os.path.join(ROOT, "ewfa-gpu_gb300", "lib", "libwfe_intpeak.so")
+    if not os.path.exists(path):
+        return None
+    L = C.CDLL(path)
+    L.wfe_int32_peak.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    ops, ms = C.c_double(0), C.c_double(0)
+    if L.wfe_int32_peak(device, 4096, 5, C.byref(ops), C.byref(ms)) != 0:
+        return None
+    return {"ops_per_s": ops.value, "best_ms": ms.value}
+
+
+def int_roofline(base, peak, launch_ms, pairs_per_launch) -> dict | None:
+    """The integer-op roofline of the dominant kernel: algorithmic integer
+    operations per launch, OPS_alg = 12 C + 8 E per pair (C wavefront cells,
+    E 16-base extend-word compares of the reference's extend over all cells
+    and the CIGAR replay, both counted by the CPU restatement over the
+    workload; 12 and 8 are the integer operations of one cell's compute and
+    one extend word in src/kernels.cu:136-152 and :84-100), divided by the
+    launch's duration and by the measured 32-bit integer issue peak."""
+    if not base or "counts" not in base or not peak:
+        return None
+    cnt = base["counts"]
+    ops_pair = (12.0 * cnt["cells"] + 8.0 * cnt["extend_words"]) / cnt["pairs"]
+    ops_launch = ops_pair * pairs_per_launch
+    achieved = ops_launch / (launch_ms * 1e-3) / 1e12
+    p = peak["ops_per_s"] / 1e12
+    return {"bound": "int32 issue", "achieved": achieved, "peak": p, "unit": "Tops/s", "frac": achieved / p,
+            "ops_per_pair": ops_pair, "ops_per_launch": ops_launch,
+            "cells_per_pair": cnt["cells"] / cnt["pairs"], "extend_words_per_pair": cnt["extend_words"] / cnt["pairs"],
+            "peak_kind": "measured: ewfa-gpu_gb300/csrc/int_peak.cu on this GPU"}
 
 
 def reference_cuda_baseline():
@@ -764,9 +802,13 @@ def main():
 
     base = None
     ref_cuda = None
+    int_peak = int32_peak(local) if rank == 0 else None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         base = cpu_baseline(ascii, pairs, os.cpu_count() or 1)
         ref_cuda = reference_cuda_baseline()
+    int_roof = int_roofline(base, int_peak, launch_ms, BATCH)
+    if base:
+        base = {k: v for k, v in base.items() if k != "counts"}
 
     if rank == 0:
         line = {
@@ -788,7 +830,8 @@ def main():
                          "kernel": f"tier_kernel tier {top}" + (" and the tiers it hands pairs on to (one timed "
                                                                      "chain)" if any(st["tier_passed"]) else ""),
                          "alg_bytes_per_launch": alg_bytes,
-                         "launch_ms": launch_ms},
+                         "launch_ms": launch_ms,
+                         "int32": int_roof},
             "gcups": {"value": value * cells_per_pair / 1e9,
                       "definition": "equivalent DP cell updates: sum of p_len * t_len per second / 1e9"},
             "cpu_baseline": base,

@@ -1,6 +1,7 @@
 """Build recipe of libwfe (sm_103a) and its tools, in-tree.
 
-    python ewfa-gpu_gb300/build.py            # lib/libwfe.so, lib/libwfe_gen.so, bin/wfe.aligner, bin/wfe.gen
+    python ewfa-gpu_gb300/build.py   # lib/libwfe.so, lib/libwfe_gen.so, lib/libwfe_intpeak.so,
+                                     # bin/wfe.aligner, bin/wfe.gen
 
 Outputs go to ewfa-gpu_gb300/_build (objects), lib/ and bin/.  Translation
 units compile in parallel; a unit is rebuilt only when it or a header it may
@@ -95,6 +96,12 @@ def build(verbose: bool = False) -> dict:
     libgen = os.path.join(LIB, "libwfe_gen.so")
     if _stale(libgen, [gen_obj]):
         _run(["gcc", "-shared", "-o", libgen, gen_obj, "-lm", "-lpthread"])
+    # the integer-issue peak probe that the benchmark's integer roofline divides by
+    peak_src = os.path.join(CSRC, "int_peak.cu")
+    libpeak = os.path.join(LIB, "libwfe_intpeak.so")
+    if _stale(libpeak, [peak_src]):
+        _run([nvcc, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-shared"] + ARCH +
+             [peak_src, "-o", libpeak])
 
     # command-line tools, linked against the shared library
     cuda_lib = os.path.join(_cuda_home(), "lib64")
