@@ -445,15 +445,9 @@ int create_context(const wfe_config* cfg, uint64_t budget5, uint64_t budget6, wf
         if ((e = cudaMalloc(&s.d_lists, kLists * B * sizeof(uint32_t))) != cudaSuccess) return bail(e);
         if ((e = cudaMalloc(&s.d_counts, sizeof(uint32_t) * kCountWords)) != cudaSuccess) return bail(e);
         if ((e = cudaMalloc(&s.d_pred, B * sizeof(uint16_t))) != cudaSuccess) return bail(e);
-        if (!host_calls) continue;
-        s.ascii_cap = B * 2u * (size_t)c.max_seq_len + 64u;
-        if ((e = cudaMalloc(&s.d_ascii, s.ascii_cap)) != cudaSuccess) return bail(e);
-        if ((e = cudaMalloc(&s.d_pairs, B * sizeof(wfe_pair))) != cudaSuccess) return bail(e);
-        if ((e = cudaMalloc(&s.d_plen, B * sizeof(uint32_t))) != cudaSuccess) return bail(e);
-        if ((e = cudaMalloc(&s.d_tlen, B * sizeof(uint32_t))) != cudaSuccess) return bail(e);
-        if ((e = cudaMalloc(&s.d_dist, B * sizeof(int32_t))) != cudaSuccess) return bail(e);
-        if ((e = cudaMalloc(&s.d_cigar, B * (size_t)c.cigar_stride + 16u)) != cudaSuccess) return bail(e);
-        if ((e = cudaMalloc(&s.d_status, B)) != cudaSuccess) return bail(e);
+        /* the staging buffers of host calls are allocated by the first call
+         * that stages (see ensure_staging) */
+        if (host_calls) s.ascii_cap = B * 2u * (size_t)c.max_seq_len + 64u;
     }
     *out = ctx;
     return WFE_OK;
@@ -749,6 +743,31 @@ private:
     std::vector<std::thread> th_;
 };
 
+/* The device buffers a stage needs to stage a batch of host inputs in and
+ * results out, allocated when a host call first stages (pinned and, with
+ * WFE_FLAG_PAGEABLE_IN_PLACE, pageable buffers are used in place and never
+ * need them).  A failed allocation leaves none of them behind. */
+int ensure_staging(wfe_ctx* ctx, Stage& s)
+{
+    if (s.d_ascii) return WFE_OK;
+    const size_t B = ctx->cfg.batch_size;
+    cudaError_t e = cudaSuccess;
+    if ((e = cudaMalloc(&s.d_ascii, s.ascii_cap)) == cudaSuccess &&
+        (e = cudaMalloc(&s.d_pairs, B * sizeof(wfe_pair))) == cudaSuccess &&
+        (e = cudaMalloc(&s.d_plen, B * sizeof(uint32_t))) == cudaSuccess &&
+        (e = cudaMalloc(&s.d_tlen, B * sizeof(uint32_t))) == cudaSuccess &&
+        (e = cudaMalloc(&s.d_dist, B * sizeof(int32_t))) == cudaSuccess &&
+        (e = cudaMalloc(&s.d_cigar, B * (size_t)ctx->cfg.cigar_stride + 16u)) == cudaSuccess &&
+        (e = cudaMalloc(&s.d_status, B)) == cudaSuccess)
+        return WFE_OK;
+    for (void** p : {(void**)&s.d_ascii, (void**)&s.d_pairs, (void**)&s.d_plen, (void**)&s.d_tlen,
+                     (void**)&s.d_dist, (void**)&s.d_cigar, (void**)&s.d_status}) {
+        cudaFree(*p);
+        *p = nullptr;
+    }
+    return fail_cuda(ctx, e);
+}
+
 int align_host(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, int8_t* cigar_out,
                uint8_t* status_out)
 {
@@ -793,6 +812,11 @@ int align_host(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, in
     }
     OutputPages out_pages(std::move(pages), std::move(unit), B, n);
     const int nstages = (c.flags & WFE_FLAG_NO_PIPELINE) ? 1 : kStages;
+    if (n > 0 && (!in_place || !out_in_place))
+        for (int i = 0; i < nstages; ++i) {
+            const int r = ensure_staging(ctx, ctx->st[i]);
+            if (r != WFE_OK) return r;
+        }
     size_t bi = 0;
     size_t nb = 0;
     for (size_t b0 = 0; b0 < n; b0 += nb, ++bi) {

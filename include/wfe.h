@@ -124,9 +124,13 @@ typedef struct wfe_stats {
 
 /* ---- lifecycle -------------------------------------------------------- */
 
-/* Create a context on cfg->device: streams, device buffers for one batch in
- * each pipeline stage, pinned staging.  Replaces the Sequences constructor
- * and GPU_memory_init (src/wavefront.cuh:458-485, src/wavefront.cu:29-108).
+/* Create a context on cfg->device: streams, the work lists of one batch in
+ * each pipeline stage, and the scratch of the tiers.  Replaces the Sequences
+ * constructor and GPU_memory_init (src/wavefront.cuh:458-485,
+ * src/wavefront.cu:29-108).  The device buffers that stage a batch of host
+ * inputs and results are allocated by the first host call that stages
+ * (buffers used in place never need them); that call returns
+ * WFE_ERR_OUT_OF_MEMORY if they do not fit.
  * Threading: a context is used by one thread at a time; different contexts
  * may be used from different threads at once.  Every call on a context makes
  * its device the calling thread's current device (as the reference's

@@ -573,14 +573,24 @@ def test_exhaustive_tiny_pairs():
 
 
 def test_allocation_failure_is_reported_and_leaves_the_device_usable():
-    """A context whose buffers cannot be allocated fails with
-    WFE_ERR_OUT_OF_MEMORY; nothing is left half-made and the next context
-    works."""
+    """Buffers that cannot be allocated give WFE_ERR_OUT_OF_MEMORY: at
+    creation (the work lists) or at the first call that stages (the staging
+    buffers); nothing is left half-made, in-place calls on such a context
+    still work, and the next context works."""
     torch_cuda()
     with pytest.raises(wfe.WfeError) as e:
-        wfe.Context(max_seq_len=2000, batch_size=200_000_000)  # 800 GB of ASCII staging per stage
+        wfe.Context(max_seq_len=300, batch_size=4_000_000_000)  # 896 GB of work lists per stage
     assert e.value.code == wfe.ERR_OUT_OF_MEMORY
     ascii, pairs = wfe.generate(2000, 150, p_min=0.05, seed=9)
+    # 200M pairs per batch: 45 GB of work lists per stage fit, 120 GB of ASCII staging does not
+    with wfe.Context(max_seq_len=300, batch_size=200_000_000, cigar_stride=152) as ctx:
+        with pytest.raises(wfe.WfeError) as e:
+            ctx.align(ascii, pairs)
+        assert e.value.code == wfe.ERR_OUT_OF_MEMORY
+        got = ctx.align(_pinned(ascii), _pinned(pairs), out=tuple(
+            _pinned(o) for o in (np.zeros(len(pairs), np.int32), np.zeros((len(pairs), 152), np.int8),
+                                 np.zeros(len(pairs), np.uint8))))
+    compare_with_oracle(ascii, pairs, 152, *got)
     with wfe.Context(max_seq_len=300, cigar_stride=152) as ctx:
         dist, cg, st = ctx.align(ascii, pairs)
     compare_with_oracle(ascii, pairs, 152, dist, cg, st)
