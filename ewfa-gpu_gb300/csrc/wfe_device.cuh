@@ -167,6 +167,85 @@ __device__ __forceinline__ void load_packed(const char* s, uint32_t len, uint2* 
     if (g == 0) Q[nw - 1].x = 0u;
 }
 
+/* Coalesced load of the pairs of a warp whose groups each align one pair:
+ * when every byte of the warp's patterns and texts lies in one span of at
+ * most SPAN aligned 16-byte blocks (pairs stored one after another), the 32
+ * lanes read the span in consecutive blocks -- whole 512-byte rows per
+ * instruction instead of one short run per group, which the CPU-GPU link
+ * serves 20% faster -- pack every block to a 32-bit word and keep the words
+ * in `words` (SPAN per warp).  Every byte read lies in a 16-byte block that
+ * holds a base of one of the pairs, as with load_packed.  Returns the
+ * span's first block address (16-aligned), or 0 when the span is too long
+ * (then nothing was read).  All 32 lanes call; p/t/lp/lt are the calling
+ * lane's group's pair (lengths 0 for a group without one). */
+template <int SPAN>
+__device__ __forceinline__ uintptr_t load_warp_span(const char* p, uint32_t lp, const char* t, uint32_t lt,
+                                                    uint32_t* words, int lane)
+{
+    unsigned long long lo = ~0ull, hi = 0ull;
+    if (lp) {
+        lo = min(lo, (unsigned long long)(uintptr_t)p);
+        hi = max(hi, (unsigned long long)(uintptr_t)p + lp);
+    }
+    if (lt) {
+        lo = min(lo, (unsigned long long)(uintptr_t)t);
+        hi = max(hi, (unsigned long long)(uintptr_t)t + lt);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(kFull, lo, o));
+        hi = max(hi, __shfl_xor_sync(kFull, hi, o));
+    }
+    if (hi == 0ull) return 0;
+    const unsigned long long a0 = lo & ~15ull;
+    const unsigned long long nblk = (hi - a0 + 15ull) >> 4;
+    if (nblk > (unsigned long long)SPAN) return 0;
+    const uint4* base = reinterpret_cast<const uint4*>((uintptr_t)a0);
+    constexpr int R = (SPAN + 31) / 32;
+    uint32_t x[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const uint32_t b = (uint32_t)(lane + 32 * r);
+        x[r] = b < nblk ? pack16(__ldg(base + b)) : 0u;
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const uint32_t b = (uint32_t)(lane + 32 * r);
+        if (b < nblk) words[b] = x[r];
+    }
+    __syncwarp();
+    return (uintptr_t)a0;
+}
+
+/* Overlapped packed pairs Q[0..nw) of a sequence of len bytes at s (see top
+ * of file) from the packed blocks of a warp span starting at a0, by a group
+ * of G lanes (words w = g, g+G, ...); Q[nw-1].x = 0.  The same words as
+ * load_packed. */
+template <int G>
+__device__ __forceinline__ void pack_from_span(const uint32_t* words, uintptr_t a0, const char* s, uint32_t len,
+                                               uint2* Q, int g)
+{
+    const uint32_t nw = (len + 15u) >> 4;
+    if (nw == 0) return;
+    const uintptr_t a = reinterpret_cast<uintptr_t>(s);
+    const uint32_t sh = (uint32_t)(a & 15u);
+    const uint32_t b0 = (uint32_t)((a - sh - a0) >> 4);
+    const uint32_t nblk = (sh + len + 15u) >> 4;
+    for (uint32_t w = (uint32_t)g; w < nw; w += G) {
+        const uint32_t x0 = words[b0 + w];
+        uint32_t W = x0;
+        if (sh != 0) {
+            const uint32_t x1 = (w + 1 < nblk) ? words[b0 + w + 1] : 0u;
+            W = __funnelshift_l(x1, x0, 2u * sh);
+        }
+        const uint32_t rem = len - 16u * w;
+        if (rem < 16u) W &= ~0u << (2u * (16u - rem));
+        Q[w].y = W;
+        if (w > 0) Q[w - 1].x = W;
+    }
+    if (g == 0) Q[nw - 1].x = 0u;
+}
+
 /* 16-base window of a packed sequence starting at base v. */
 __device__ __forceinline__ uint32_t window(const uint2* Q, int v)
 {

@@ -149,10 +149,17 @@ size_t group_smem_bytes(uint32_t max_len, uint32_t cigar_stride)
     return 16u * (size_t)seq_words_for(max_len) + T::chain_bytes + union_bytes<T>(cigar_stride);
 }
 
+/* The tiers with several pairs per warp also keep, per warp, the packed
+ * blocks of a coalesced span load of the warp's pairs (load_warp_span):
+ * 160 blocks, 2,560 bytes of input, enough for 8 pairs of 150 bases stored
+ * one after another with their file's line marks. */
+constexpr int kSpanWords = 160;
+
 template <class T>
 size_t cta_smem_bytes(uint32_t max_len, uint32_t cigar_stride)
 {
-    return group_smem_bytes<T>(max_len, cigar_stride) * (size_t)(kWarps * T::GPW);
+    const size_t span = T::G < 32 ? (size_t)kWarps * kSpanWords * sizeof(uint32_t) : 0u;
+    return group_smem_bytes<T>(max_len, cigar_stride) * (size_t)(kWarps * T::GPW) + span;
 }
 
 /* The alignment kernel of a tier, in two forms with one body (tier_body):
@@ -338,8 +345,21 @@ __device__ __forceinline__ void tier_body(const AlignLaunch& A, uint32_t seq_wor
         /* a prediction launch aligns only the first kPredictPrefix bases */
         const uint32_t lp = state == ST_RUN ? (PREDICT ? min(pr.plen, (uint32_t)kPredictPrefix) : pr.plen) : 0u;
         const uint32_t lt = state == ST_RUN ? (PREDICT ? min(pr.tlen, (uint32_t)kPredictPrefix) : pr.tlen) : 0u;
-        load_packed<G, T::RMAX>(pr.p, lp, QP, g, gmask);
-        load_packed<G, T::RMAX>(pr.t, lt, QT, g, gmask);
+        if constexpr (G < 32) {
+            /* the warp's 8 pairs in one coalesced span when they lie together */
+            uint32_t* span = reinterpret_cast<uint32_t*>(smem + (size_t)(kWarps * GPW) * gbytes) + warp * kSpanWords;
+            const uintptr_t a0 = load_warp_span<kSpanWords>(pr.p, lp, pr.t, lt, span, lane);
+            if (a0) {
+                pack_from_span<G>(span, a0, pr.p, lp, QP, g);
+                pack_from_span<G>(span, a0, pr.t, lt, QT, g);
+            } else {
+                load_packed<G, T::RMAX>(pr.p, lp, QP, g, gmask);
+                load_packed<G, T::RMAX>(pr.t, lt, QT, g, gmask);
+            }
+        } else {
+            load_packed<G, T::RMAX>(pr.p, lp, QP, g, gmask);
+            load_packed<G, T::RMAX>(pr.t, lt, QT, g, gmask);
+        }
         __syncwarp();
 
         const int plen = (int)lp, tlen = (int)lt, kt = tlen - plen;
@@ -724,7 +744,7 @@ cudaError_t launch(const AlignLaunch& a, int grid, cudaStream_t s)
 {
     const uint32_t sw = seq_words_for(a.max_len);
     const size_t gb = group_smem_bytes<T>(a.max_len, a.cigar_stride);
-    const size_t smem = gb * (size_t)(kWarps * T::GPW);
+    const size_t smem = cta_smem_bytes<T>(a.max_len, a.cigar_stride);
     if (smem > 227u * 1024u) return cudaErrorInvalidValue;
     if (!T::SMEM_OPS && a.ops_scratch_bytes < T::ops_bytes * (size_t)grid * (kWarps * T::GPW))
         return cudaErrorInvalidValue;
@@ -971,7 +991,7 @@ cudaError_t launch_predict(const Layout& L, uint32_t n, uint32_t max_len, uint16
     if (n == 0) return cudaSuccess;
     const uint32_t plen = std::min<uint32_t>(max_len, (uint32_t)kPredictPrefix);
     const size_t gb = group_smem_bytes<T0>(plen, 0);
-    const size_t smem = gb * (size_t)(kWarps * T0::GPW);
+    const size_t smem = cta_smem_bytes<T0>(plen, 0);
     cudaError_t e = allow_smem((const void*)tier_kernel_bounded<T0, true>, smem);
     if (e != cudaSuccess) return e;
     AlignLaunch a{};
