@@ -697,14 +697,26 @@ public:
         nb_ = batch_ ? (n_ + batch_ - 1) / batch_ : 0;
         if (r_.empty() || missing * HostRange::page() < (8u << 20) || nb_ == 0) return;
         const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-        nthreads_ = std::min(8u, hw);
-        left_.reset(new std::atomic<unsigned>[nb_]);
+        const unsigned want = std::min(8u, hw);
+        left_.reset(new (std::nothrow) std::atomic<unsigned>[nb_]);
+        if (!left_) return;
+        /* the helpers wait for `go_`, so that the stripes are cut for the
+         * threads that could actually be started (none: ready() touches) */
+        for (unsigned t = 0; t < want; ++t) {
+            try {
+                th_.emplace_back([this, t] { run(t); });
+            } catch (...) {
+                break;
+            }
+        }
+        nthreads_ = (unsigned)th_.size();
         for (size_t b = 0; b < nb_; ++b) left_[b].store(nthreads_);
-        for (unsigned t = 0; t < nthreads_; ++t) th_.emplace_back([this, t] { run(t); });
+        go_.store(true, std::memory_order_release);
     }
     ~OutputPages()
     {
         stop_.store(true);
+        go_.store(true, std::memory_order_release);
         for (auto& x : th_) x.join();
     }
     /* batch b's output pages are present */
@@ -729,6 +741,7 @@ private:
     }
     void run(unsigned t)
     {
+        while (!go_.load(std::memory_order_acquire)) std::this_thread::yield();
         for (size_t b = 0; b < nb_ && !stop_.load(std::memory_order_relaxed); ++b) {
             stripe(b, t, nthreads_);
             left_[b].fetch_sub(1, std::memory_order_release);
@@ -740,6 +753,7 @@ private:
     unsigned nthreads_ = 0;
     std::unique_ptr<std::atomic<unsigned>[]> left_;
     std::atomic<bool> stop_{false};
+    std::atomic<bool> go_{false};
     std::vector<std::thread> th_;
 };
 
