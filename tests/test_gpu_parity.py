@@ -221,6 +221,72 @@ def test_unaligned_offsets_and_batches():
     compare_with_oracle(ascii, pairs, 152, d1, c1, s1)
 
 
+def test_warp_span_layouts():
+    """Tier 0 loads a warp's 8 pairs as one coalesced span when they lie
+    within 2,560 bytes.  Layouts that exercise it: each warp's 16 sequences
+    stored in shuffled order (texts before patterns), random gaps and
+    alignments, empty sequences, spans on both sides of the limit, and warps
+    with one sequence far away (the per-group load).  Results equal the
+    oracle's and the back-to-back layout's, staged and read in place."""
+    rng = np.random.default_rng(23)
+    ascii, pairs = wfe.generate(4096, 150, p_min=0.05, seed=23)
+    seqs = [(ascii[q["p_off"]: q["p_off"] + q["p_len"]].tobytes(), ascii[q["t_off"]: q["t_off"] + q["t_len"]].tobytes())
+            for q in pairs]
+    for i in rng.choice(len(seqs), 40, replace=False):
+        seqs[i] = (b"", seqs[i][1]) if i % 2 else (seqs[i][0], b"")
+
+    def filler(k):
+        return rng.choice(np.frombuffer(b"ACGT", np.uint8), size=k).tobytes()
+
+    buf = bytearray(filler(int(rng.integers(0, 16))))
+    far = bytearray()
+    far_at = {}
+    offs = np.zeros((len(seqs), 2), np.uint64)
+    for w0 in range(0, len(seqs), 8):
+        w = w0 // 8
+        pieces = [(i, s) for i in range(w0, w0 + 8) for s in (0, 1)]
+        order = rng.permutation(len(pieces))
+        start = len(buf)
+        for j, o in enumerate(order):
+            i, s = pieces[o]
+            if w % 16 == 5 and j == len(order) - 1:
+                far_at[(i, s)] = len(far)   # placed 10 KB after the main buffer below
+                far += seqs[i][s] + filler(7)
+                continue
+            if w % 7 == 3 and j == len(order) - 1:
+                # pad so that the span lands within 40 bytes either side of 2,560
+                span = len(buf) - start + len(seqs[i][s])
+                buf += filler(max(0, 2540 + int(rng.integers(0, 41)) - span))
+            else:
+                buf += filler(int(rng.integers(0, 6)))
+            offs[i, s] = len(buf)
+            buf += seqs[i][s]
+    base_far = len(buf) + 10000
+    buf += filler(10000) + far + b"\0" * 64
+    for (i, s), at in far_at.items():
+        offs[i, s] = base_far + at
+    big = np.frombuffer(bytes(buf), np.uint8).copy()
+    lay = np.zeros(len(seqs), wfe.PAIR_DTYPE)
+    lay["p_off"], lay["t_off"] = offs[:, 0], offs[:, 1]
+    lay["p_len"] = [len(p) for p, _ in seqs]
+    lay["t_len"] = [len(t) for _, t in seqs]
+    for i in range(0, len(seqs), 97):   # the layout holds the sequences it claims
+        assert big[lay["p_off"][i]: lay["p_off"][i] + lay["p_len"][i]].tobytes() == seqs[i][0]
+        assert big[lay["t_off"][i]: lay["t_off"][i] + lay["t_len"][i]].tobytes() == seqs[i][1]
+
+    flat_ascii, flat_pairs = wfe.pairs_from_list(seqs)
+    with wfe.Context(max_seq_len=300, batch_size=1000, cigar_stride=152) as ctx:
+        want = ctx.align(flat_ascii, flat_pairs)
+        staged = ctx.align(big, lay)
+        in_place = ctx.align(_pinned(big), _pinned(lay))
+        assert ctx.stats()["mapped_batches"] == 5
+    for got in (staged, in_place):
+        np.testing.assert_array_equal(got[0], want[0])
+        np.testing.assert_array_equal(got[2], want[2])
+        assert_same_cigars(got[1], want[1])
+    compare_with_oracle(big, lay, 152, *in_place)
+
+
 def test_scattered_pairs_gather_path():
     """Pairs that point all over a large buffer go through the pinned gather."""
     ascii, pairs = wfe.generate(2000, 150, p_min=0.05, seed=9)
