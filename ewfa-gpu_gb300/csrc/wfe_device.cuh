@@ -202,16 +202,18 @@ __device__ __forceinline__ uintptr_t load_warp_span(const char* p, uint32_t lp, 
     if (nblk > (unsigned long long)SPAN) return 0;
     const uint4* base = reinterpret_cast<const uint4*>((uintptr_t)a0);
     constexpr int R = (SPAN + 31) / 32;
-    uint32_t x[R];
+    /* every load of the lane is issued before the first is used: over the
+     * CPU-GPU link each round trip costs microseconds */
+    uint4 v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         const uint32_t b = (uint32_t)(lane + 32 * r);
-        x[r] = b < nblk ? pack16(__ldg(base + b)) : 0u;
+        v[r] = b < nblk ? __ldg(base + b) : make_uint4(0u, 0u, 0u, 0u);
     }
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         const uint32_t b = (uint32_t)(lane + 32 * r);
-        if (b < nblk) words[b] = x[r];
+        if (b < nblk) words[b] = pack16(v[r]);
     }
     __syncwarp();
     return (uintptr_t)a0;
