@@ -58,19 +58,29 @@ struct PairRef {
     bool in_range;          /* both sequences lie inside the checked buffer */
 };
 
+/* Where the bases of a pair of the descriptor layout live, from its
+ * descriptor d. */
+__device__ __forceinline__ PairRef pair_from_desc(const Layout& L, const wfe_pair& d)
+{
+    PairRef r;
+    r.p = L.ascii + (d.p_off - L.base_off);
+    r.t = L.ascii + (d.t_off - L.base_off);
+    r.plen = d.p_len;
+    r.tlen = d.t_len;
+    r.in_range = true;
+    if (L.ascii_bytes)
+        r.in_range = d.p_off <= L.ascii_bytes && d.p_len <= L.ascii_bytes - d.p_off &&
+                     d.t_off <= L.ascii_bytes && d.t_len <= L.ascii_bytes - d.t_off;
+    return r;
+}
+
 __device__ __forceinline__ PairRef get_pair(const Layout& L, uint32_t i)
 {
     PairRef r;
     r.in_range = true;
     if (L.pairs) {
         const wfe_pair d = L.pairs[i];
-        r.p = L.ascii + (d.p_off - L.base_off);
-        r.t = L.ascii + (d.t_off - L.base_off);
-        r.plen = d.p_len;
-        r.tlen = d.t_len;
-        if (L.ascii_bytes)
-            r.in_range = d.p_off <= L.ascii_bytes && d.p_len <= L.ascii_bytes - d.p_off &&
-                         d.t_off <= L.ascii_bytes && d.t_len <= L.ascii_bytes - d.t_off;
+        r = pair_from_desc(L, d);
     } else {
         r.p = L.ascii + 2ull * i * L.stride;
         r.t = r.p + L.stride;
