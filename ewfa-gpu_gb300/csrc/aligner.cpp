@@ -207,6 +207,7 @@ int main(int argc, char** argv)
     auto pair_at = [&](size_t i) -> const wfe_pair* { return i < pf.n ? pf.pairs + i : tail.data() + (i - pf.n); };
     const uint32_t stride = (uint32_t)(seq_len + (4 - seq_len % 4)); /* cigar_max_len */
 
+    const bool keep = print || check;
     const double t0 = now_s();
     std::vector<Share> shares((size_t)threads);
     auto worker = [&](size_t t) {
@@ -233,19 +234,26 @@ int main(int argc, char** argv)
             sh.what = "wfe_create";
             return;
         }
-        sh.dist.reset(new int32_t[sh.n]);
-        sh.cigar.reset(new int8_t[sh.n * stride]);
-        sh.status.reset(new uint8_t[sh.n]);
         /* the pairs of this share: in the file's pinned descriptors, or the
          * empty tail */
-        if (sh.first + sh.n <= pf.n) {
-            sh.rc = wfe_align(ctx, pf.ascii, pf.ascii_bytes, pf.pairs + sh.first, sh.n, sh.dist.get(), sh.cigar.get(),
-                              sh.status.get());
-        } else {
-            std::vector<wfe_pair> mine(sh.n);
+        std::vector<wfe_pair> mine;
+        const wfe_pair* src = pf.pairs + sh.first;
+        if (sh.first + sh.n > pf.n) {
+            mine.resize(sh.n);
             for (size_t i = 0; i < sh.n; ++i) mine[i] = *pair_at(sh.first + i);
-            sh.rc = wfe_align(ctx, pf.ascii, pf.ascii_bytes, mine.data(), sh.n, sh.dist.get(), sh.cigar.get(),
-                              sh.status.get());
+            src = mine.data();
+        }
+        /* Results that are printed or checked are kept for the whole share.
+         * Otherwise, as the reference keeps one batch of CIGARs on the host
+         * (src/wavefront.cu:267-300), a window of two batches (both
+         * pipeline stages busy) is written over and over. */
+        const size_t window = keep ? sh.n : std::min(sh.n, 2 * b);
+        sh.dist.reset(new int32_t[window]);
+        sh.cigar.reset(new int8_t[window * stride]);
+        sh.status.reset(new uint8_t[window]);
+        for (size_t c0 = 0; c0 < sh.n && sh.rc == WFE_OK; c0 += window) {
+            sh.rc = wfe_align(ctx, pf.ascii, pf.ascii_bytes, src + c0, std::min(window, sh.n - c0), sh.dist.get(),
+                              sh.cigar.get(), sh.status.get());
         }
         if (sh.rc != WFE_OK) sh.what = "wfe_align";
         wfe_destroy(ctx);
