@@ -1,9 +1,9 @@
 /*
  * wfe_oracle.c -- CPU restatement of the eWFA-GPU alignment path.
  *
- * TEST INFRASTRUCTURE ONLY (the checker and the CPU baseline); the product
- * library never links it.  See wfe_oracle.h for the reference semantics kept
- * and the file:line each function follows.
+ * TEST INFRASTRUCTURE ONLY (the oracle of the parity tests and the CPU
+ * baseline); the product library never links it.  See wfe_oracle.h for the
+ * reference semantics kept and the file:line each function follows.
  */
 #define _GNU_SOURCE
 #include "wfe_oracle.h"

@@ -3,7 +3,8 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product library links or calls
  * this code; only the test-suite, the smoke check and the CPU-baseline leg of
- * bench.py load it, and only as the checker / the CPU baseline.
+ * bench.py load it, and only as the oracle the GPU results are compared with,
+ * or as the CPU baseline.
  *
  * Every function restates one piece of the reference (quim0/eWFA-GPU) and
  * cites the file:line it follows.  The restatement is pinned against the
