@@ -319,47 +319,19 @@ __device__ __forceinline__ int8_t op_letter(int op)
     return op == kOpDel ? (int8_t)'D' : (op == kOpSub ? (int8_t)'X' : (int8_t)'I');
 }
 
-/* Forward replay of an operation chain into an encoded CIGAR
- * (src/kernels.cu:397-498) by a group of G lanes.  chain[d] is the operation
- * of score d+1.
- *   1. In order of d, the run of M bases before operation d comes from a
- *      group-parallel extend from (k, off), starting at (0, 0); runs[d]
- *      keeps it (lane 0 writes).
- *   2. In parallel, lane g takes steps g, g+G, ...: each step's bytes are its
- *      run as chunks of at most 127 (-127, ..., -(run % 127)) and then its
- *      operation letter; an inclusive shuffle scan over the group gives the
- *      step's first byte, and every lane writes its own bytes into buf (cap
- *      bytes; positions past cap are counted but not written).
- * Returns the full CIGAR length on every lane, or -1 - length if the chain
- * holds a code other than INS/SUB/DEL: the CIGAR then stops after that
- * step's run, like the reference's "Incorrect backtrace" exit
- * (src/kernels.cu:471-478). */
+/* Encoded CIGAR bytes of steps 0..last of a replayed chain
+ * (src/kernels.cu:397-498), by a group of G lanes: runs[d] is the run of M
+ * bases before operation d (chain[d], the operation of score d+1).  Lane g
+ * takes steps g, g+G, ...: each step's bytes are its run as chunks of at
+ * most 127 (-127, ..., -(run % 127)) and then its operation letter (none for
+ * step D and for a step at bad_at); an inclusive shuffle scan over the group
+ * gives the step's first byte, and every lane writes its own bytes into buf
+ * (cap bytes; positions past cap are counted but not written).  Returns the
+ * full length on every lane. */
 template <int G>
-__device__ __forceinline__ int replay_chain(const uint2* QP, const uint2* QT, int plen, int tlen,
-                                            const uint8_t* chain, int D, int* runs, int8_t* buf,
-                                            uint32_t cap, int g, int grp, unsigned gmask)
+__device__ __forceinline__ int encode_runs(const int* runs, const uint8_t* chain, int D, int last, int bad_at,
+                                           int8_t* buf, uint32_t cap, int g, unsigned gmask)
 {
-    int k = 0, off = 0, bad_at = -1;
-    for (int d = 0; d <= D; ++d) {
-        const int run = group_extend<G>(QP, QT, plen, tlen, k, off, g, grp, gmask);
-        if (g == 0) runs[d] = run;
-        off += run;
-        if (d == D) break;
-        const int op = chain[d];
-        if (op == kOpDel) {
-            --k;
-        } else if (op == kOpSub) {
-            ++off;
-        } else if (op == kOpIns) {
-            ++k;
-            ++off;
-        } else {
-            bad_at = d;
-            break;
-        }
-    }
-    const int last = bad_at >= 0 ? bad_at : D;
-    __syncwarp(gmask);
     int total = 0;
     for (int base = 0; base <= last; base += G) {
         const int d = base + g;
@@ -392,6 +364,47 @@ __device__ __forceinline__ int replay_chain(const uint2* QP, const uint2* QT, in
         }
         total += __shfl_sync(gmask, x, G - 1, G);
     }
+    return total;
+}
+
+/* Forward replay of an operation chain into an encoded CIGAR
+ * (src/kernels.cu:397-498) by a group of G lanes.  chain[d] is the operation
+ * of score d+1.
+ *   1. In order of d, the run of M bases before operation d comes from a
+ *      group-parallel extend from (k, off), starting at (0, 0); runs[d]
+ *      keeps it (lane 0 writes).
+ *   2. encode_runs writes the bytes.
+ * Returns the full CIGAR length on every lane, or -1 - length if the chain
+ * holds a code other than INS/SUB/DEL: the CIGAR then stops after that
+ * step's run, like the reference's "Incorrect backtrace" exit
+ * (src/kernels.cu:471-478). */
+template <int G>
+__device__ __forceinline__ int replay_chain(const uint2* QP, const uint2* QT, int plen, int tlen,
+                                            const uint8_t* chain, int D, int* runs, int8_t* buf,
+                                            uint32_t cap, int g, int grp, unsigned gmask)
+{
+    int k = 0, off = 0, bad_at = -1;
+    for (int d = 0; d <= D; ++d) {
+        const int run = group_extend<G>(QP, QT, plen, tlen, k, off, g, grp, gmask);
+        if (g == 0) runs[d] = run;
+        off += run;
+        if (d == D) break;
+        const int op = chain[d];
+        if (op == kOpDel) {
+            --k;
+        } else if (op == kOpSub) {
+            ++off;
+        } else if (op == kOpIns) {
+            ++k;
+            ++off;
+        } else {
+            bad_at = d;
+            break;
+        }
+    }
+    const int last = bad_at >= 0 ? bad_at : D;
+    __syncwarp(gmask);
+    const int total = encode_runs<G>(runs, chain, D, last, bad_at, buf, cap, g, gmask);
     return bad_at >= 0 ? -1 - total : total;
 }
 
