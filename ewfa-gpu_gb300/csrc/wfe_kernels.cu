@@ -810,7 +810,53 @@ __global__ void __launch_bounds__(256) classify_kernel(Layout L, uint32_t n, Buc
 }
 
 /* ------------------------------------------------------------------------ */
-/* Standalone packer: one warp per sequence (src/kernels.cu:313-394). */
+/* Standalone packer (src/kernels.cu:313-394): one thread per kPackWords
+ * output words.  Thread t writes words kPackWords*j .. kPackWords*j +
+ * kPackWords-1 of sequence t / ceil(wps/kPackWords) (pattern of pair i at
+ * 2i, text at 2i+1), j = t % ceil(wps/kPackWords), from the kPackWords+1
+ * aligned 16-byte blocks that hold their bases, each packed once; the
+ * threads of a sequence read its blocks and descriptor through L1, so the
+ * ASCII is read from DRAM about once and the words are written with
+ * coalesced stores.  For 2 n ceil(wps/kPackWords) < 2^32. */
+constexpr int kPackWords = 4;
+__global__ void __launch_bounds__(256)
+pack_words_kernel(Layout L, uint32_t n, uint32_t* out, uint32_t wps)
+{
+    const uint32_t gps = (wps + kPackWords - 1u) / kPackWords;
+    const uint32_t total = 2u * n * gps;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        const uint32_t sidx = t / gps, w0 = kPackWords * (t - sidx * gps);
+        const PairRef pr = get_pair(L, sidx >> 1);
+        const char* s = (sidx & 1u) ? pr.t : pr.p;
+        const uint32_t len = (sidx & 1u) ? pr.tlen : pr.plen;
+        const uint32_t nw = (len + 15u) >> 4;
+        const uintptr_t a = reinterpret_cast<uintptr_t>(s);
+        const uint32_t sh = (uint32_t)(a & 15u);
+        const uint4* base = reinterpret_cast<const uint4*>(a - sh);
+        const uint32_t nblk = (sh + len + 15u) >> 4;
+        uint4 v[kPackWords + 1];
+#pragma unroll
+        for (int r = 0; r <= kPackWords; ++r) v[r] = w0 + r < nblk ? __ldg(base + w0 + r) : make_uint4(0u, 0u, 0u, 0u);
+        uint32_t x[kPackWords + 1];
+#pragma unroll
+        for (int r = 0; r <= kPackWords; ++r) x[r] = pack16(v[r]);
+        uint32_t* dst = out + (size_t)sidx * wps;
+#pragma unroll
+        for (int r = 0; r < kPackWords; ++r) {
+            const uint32_t w = w0 + (uint32_t)r;
+            if (w >= wps) break;
+            uint32_t W = 0;
+            if (w < nw) {
+                W = sh ? __funnelshift_l(x[r + 1], x[r], 2u * sh) : x[r];
+                const uint32_t rem = len - 16u * w;
+                if (rem < 16u) W &= ~0u << (2u * (16u - rem));
+            }
+            dst[w] = W;
+        }
+    }
+}
+
+/* The same words, one warp per sequence: for outputs of 2^32 words or more. */
 __global__ void __launch_bounds__(256)
 pack_kernel(Layout L, uint32_t n, uint32_t* out, uint32_t wps)
 {
@@ -1009,6 +1055,18 @@ cudaError_t launch_predict(const Layout& L, uint32_t n, uint32_t max_len, uint16
 cudaError_t launch_pack(const Layout& L, uint32_t n, uint32_t* words, uint32_t wps, cudaStream_t s)
 {
     if (n == 0) return cudaSuccess;
+    const uint64_t total = 2ull * n * ((wps + kPackWords - 1u) / kPackWords);
+    if (total < (1ull << 32)) {
+        int dev = 0, sms = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                      cudaSuccess)
+            return cudaErrorInvalidValue;
+        /* 8 blocks of 256 per SM, each thread looping over words */
+        const uint32_t blocks = (uint32_t)std::max<uint64_t>(
+            1u, std::min<uint64_t>((total + 255u) / 256u, (uint64_t)sms * 8u));
+        pack_words_kernel<<<blocks, 256, 0, s>>>(L, n, words, wps);
+        return cudaGetLastError();
+    }
     const uint32_t warps = 2u * n;
     const uint32_t blocks = std::min<uint32_t>((warps + 7u) / 8u, 65535u * 16u);
     pack_kernel<<<blocks, 256, 0, s>>>(L, n, words, wps);
