@@ -878,9 +878,10 @@ pack_kernel(Layout L, uint32_t n, uint32_t* out, uint32_t wps)
 }
 
 /* ------------------------------------------------------------------------ */
-/* CIGARs from 128-bit histories (src/kernels.cu:397-625): one group of 8
- * lanes per pair. */
-constexpr int kHG = 8;
+/* CIGARs from 128-bit histories (src/kernels.cu:397-625): one group of 4
+ * lanes per pair, 8 pairs per warp (a history holds at most 63 operations,
+ * and 4 lanes extend 64 bases per trip). */
+constexpr int kHG = 4;
 
 __global__ void __launch_bounds__(kThreads)
 history_cigar_kernel(Layout L, uint32_t n, uint32_t max_len, const int32_t* dist,
@@ -913,8 +914,8 @@ history_cigar_kernel(Layout L, uint32_t n, uint32_t max_len, const int32_t* dist
             }
             continue;
         }
-        load_packed<G, 3>(pr.p, pr.plen, QP, g, gmask);
-        load_packed<G, 3>(pr.t, pr.tlen, QT, g, gmask);
+        load_packed<G, (G == 4 ? 5 : 3)>(pr.p, pr.plen, QP, g, gmask);
+        load_packed<G, (G == 4 ? 5 : 3)>(pr.t, pr.tlen, QT, g, gmask);
         const uint64_t w0 = hist[2u * pi], w1 = hist[2u * pi + 1u];
         for (int d = g; d < D; d += G)
             chain[d] = (uint8_t)(((d < 32 ? w0 : w1) >> (2 * (d & 31))) & 3u);
