@@ -51,6 +51,13 @@ struct Stage {
     uint16_t* d_pred = nullptr;   /* predicted prefix distances */
     char* h_stage = nullptr;      /* pinned gather buffer for scattered inputs */
     wfe_pair* h_pairs = nullptr;  /* pinned descriptors of a gathered batch */
+    /* Scratch of tiers 3-6 owned by this stage (stage 1 only; stage 0 uses
+     * the context's): the chains of the two stages run at the same time, and
+     * a tier's CTAs index their scratch by blockIdx, so two grids of one tier
+     * must not share it. */
+    unsigned char* own_ops_scratch = nullptr;
+    unsigned char* own_long_scratch[kNumTiers] = {};
+    bool own_scratch = false;
 };
 
 thread_local int g_last_create_error = 0;
@@ -162,6 +169,8 @@ void free_stage(Stage& s)
     cudaFree(s.d_pred);
     cudaFreeHost(s.h_stage);
     cudaFreeHost(s.h_pairs);
+    cudaFree(s.own_ops_scratch);
+    for (auto p : s.own_long_scratch) cudaFree(p);
     if (s.stream) cudaStreamDestroy(s.stream);
     s = Stage();
 }
@@ -242,13 +251,14 @@ int launch_bucket(wfe_ctx* ctx, Stage& st, const BucketPlan& bp, int bucket_inde
     a.status = status;
     a.max_distance = c.max_distance;
     a.max_len = bp.max_len;
-    a.ops_scratch = ctx->d_ops_scratch;
+    a.ops_scratch = st.own_ops_scratch ? st.own_ops_scratch : ctx->d_ops_scratch;
     a.ops_scratch_bytes = ctx->ops_scratch_bytes;
     a.tier = t;
     const int last = chain_end(c, t, bp.last_tier);
     a.chain.last_tier = last;
     for (int u = 0; u < kNumTiers; ++u) {
         a.chain.shape[u] = bp.shape[u];
+        if (st.own_long_scratch[u]) a.chain.shape[u].scratch = st.own_long_scratch[u];
         a.chain.list[u] = lists + (size_t)u * B;
     }
     a.chain.counts = words;
@@ -782,6 +792,30 @@ int ensure_staging(wfe_ctx* ctx, Stage& s)
     return fail_cuda(ctx, e);
 }
 
+/* Stage 1's own scratch of tiers 3-6, the size of the context's, allocated
+ * when a host call first runs two batches at once.  A failed allocation
+ * leaves none of it behind. */
+int ensure_stage_scratch(wfe_ctx* ctx, Stage& s)
+{
+    if (s.own_scratch) return WFE_OK;
+    cudaError_t e = cudaSuccess;
+    if (ctx->d_ops_scratch) e = cudaMalloc(&s.own_ops_scratch, ctx->ops_scratch_bytes);
+    for (int t = 5; t < kNumTiers && e == cudaSuccess; ++t)
+        if (ctx->d_long_scratch[t])
+            e = cudaMalloc(&s.own_long_scratch[t], (size_t)ctx->long_slab[t] * (size_t)ctx->scratch_ctas[t]);
+    if (e != cudaSuccess) {
+        cudaFree(s.own_ops_scratch);
+        s.own_ops_scratch = nullptr;
+        for (auto& p : s.own_long_scratch) {
+            cudaFree(p);
+            p = nullptr;
+        }
+        return fail_cuda(ctx, e);
+    }
+    s.own_scratch = true;
+    return WFE_OK;
+}
+
 int align_host(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, int8_t* cigar_out,
                uint8_t* status_out)
 {
@@ -825,7 +859,10 @@ int align_host(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, in
         if (r_status.p) pages.push_back(std::move(r_status)), unit.push_back(1u);
     }
     OutputPages out_pages(std::move(pages), std::move(unit), B, n);
-    const int nstages = (c.flags & WFE_FLAG_NO_PIPELINE) ? 1 : kStages;
+    int nstages = (c.flags & WFE_FLAG_NO_PIPELINE) ? 1 : kStages;
+    /* a second batch in flight needs the second stage's own tier scratch;
+     * without it the call runs one batch at a time */
+    if (nstages > 1 && n > B && ensure_stage_scratch(ctx, ctx->st[1]) != WFE_OK) nstages = 1;
     if (n > 0 && (!in_place || !out_in_place))
         for (int i = 0; i < nstages; ++i) {
             const int r = ensure_staging(ctx, ctx->st[i]);

@@ -245,8 +245,11 @@ int wfe_align_strided(wfe_ctx* ctx, const char* ascii, size_t stride,
  * sequence (sequences are read in aligned 16-byte blocks).  A tier that a
  * kernel failed to launch on the device (its pairs are left unaligned) is
  * reported as WFE_ERR_CUDA by the next call on the context; wfe_align and
- * wfe_align_strided report it themselves.  Replaces the kernel chain
- * WF_edit_distance -> generate_cigars (src/wavefront.cu:203-260). */
+ * wfe_align_strided report it themselves.  The device calls of a context
+ * share its work lists and scratch: enqueue them on one stream (or order
+ * them), and synchronise that stream before a host call on the context.
+ * Replaces the kernel chain WF_edit_distance -> generate_cigars
+ * (src/wavefront.cu:203-260). */
 int wfe_align_device(wfe_ctx* ctx, const char* d_ascii,
                      const wfe_pair* d_pairs, size_t n, uint32_t max_len,
                      int32_t* d_dist, int8_t* d_cigar, uint8_t* d_status,

@@ -221,6 +221,22 @@ def test_unaligned_offsets_and_batches():
     compare_with_oracle(ascii, pairs, 152, d1, c1, s1)
 
 
+def test_two_stages_in_the_scratch_tiers():
+    """Host calls keep two batches in flight on two streams; with small
+    batches of pairs whose distances need tiers 3-6, both stages' chains run
+    those tiers at the same time, each on its own scratch."""
+    torch_cuda()
+    ascii, pairs = wfe.generate(3000, 300, 2600, p_min=0.2, p_max=0.45, seed=41)
+    with wfe.Context(max_seq_len=2700, batch_size=150, cigar_stride=3000) as ctx:
+        d1, c1, s1 = ctx.align(ascii, pairs)
+        st = ctx.stats()
+        assert st["batches"] == 20 and st["tier_passed"][3] > 0 and st["tier_passed"][4] > 0, st
+        d2, c2, s2 = ctx.align(_pinned(ascii), _pinned(pairs))
+    np.testing.assert_array_equal(d1, d2)
+    assert_same_cigars(c1, c2)
+    compare_with_oracle(ascii, pairs, 3000, d1, c1, s1)
+
+
 def test_warp_span_layouts():
     """Tier 0 loads a warp's 8 pairs as one coalesced span when they lie
     within 2,560 bytes.  Layouts that exercise it: each warp's 16 sequences
