@@ -682,12 +682,16 @@ void* mapped_address(const void* p, size_t bytes, bool write, bool pageable, Hos
     }
     if (at.type == cudaMemoryTypeHost) return at.devicePointer;
     if (at.type != cudaMemoryTypeUnregistered || !pageable || bytes == 0) return nullptr;
-    HostRange r;
-    if (!r.map(p, bytes, write)) return nullptr;
-    if (write) {
-        *range = std::move(r);
-    } else if (r.missing) {
-        r.touch(0, bytes);
+    try {
+        HostRange r;
+        if (!r.map(p, bytes, write)) return nullptr;
+        if (write) {
+            *range = std::move(r);
+        } else if (r.missing) {
+            r.touch(0, bytes);
+        }
+    } catch (const std::bad_alloc&) {
+        return nullptr; /* no room for the page map: staged */
     }
     return const_cast<void*>(p);
 }
@@ -816,8 +820,24 @@ int ensure_stage_scratch(wfe_ctx* ctx, Stage& s)
     return WFE_OK;
 }
 
+int align_host_checked(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, int8_t* cigar_out,
+                       uint8_t* status_out);
+
+/* The host-buffer calls: no C++ exception crosses the C ABI. */
 int align_host(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, int8_t* cigar_out,
                uint8_t* status_out)
+{
+    try {
+        return align_host_checked(ctx, job, n, dist_out, cigar_out, status_out);
+    } catch (const std::bad_alloc&) {
+        return WFE_ERR_OUT_OF_MEMORY;
+    } catch (...) {
+        return WFE_ERR_INTERNAL;
+    }
+}
+
+int align_host_checked(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, int8_t* cigar_out,
+                       uint8_t* status_out)
 {
     const wfe_config& c = ctx->cfg;
     if (c.flags & WFE_FLAG_DEVICE_ONLY) return WFE_ERR_INVALID_ARGUMENT;

@@ -593,7 +593,14 @@ int wfe_submit(wfe_server* s, const char* ascii, size_t ascii_bytes, const wfe_p
         return WFE_ERR_INVALID_ARGUMENT;
     }
     r->id = s->next_id++;
-    s->tickets[r->id] = r;
+    try { /* no C++ exception crosses the C ABI */
+        s->tickets[r->id] = r;
+        if (n > 0) s->pending.push_back(r);
+    } catch (const std::bad_alloc&) {
+        s->tickets.erase(r->id);
+        delete r;
+        return WFE_ERR_OUT_OF_MEMORY;
+    }
     *ticket = r->id;
     if (n == 0) {
         r->done = true;
@@ -602,7 +609,6 @@ int wfe_submit(wfe_server* s, const char* ascii, size_t ascii_bytes, const wfe_p
         s->cv_done.notify_all();
         return WFE_OK;
     }
-    s->pending.push_back(r);
     s->cv_work.notify_one();
     return WFE_OK;
 }
