@@ -76,6 +76,9 @@ def test_cli_prints_the_oracle_cigars(tmp_path):
     r2 = _run("-f", f, "-n", n, "-l", 150, "-b", 400, "-t", 3, "-p", check=True)
     got2 = _printed(r2.stdout)
     assert [got2[i] for i in range(n)] == want
+    # without -p or --check the share is aligned in windows of two batches
+    r3 = _run("-f", f, "-n", n, "-l", 150, "-b", 400, "-t", 2, check=True)
+    assert "Aligned executed. Wall time" in r3.stdout and not _printed(r3.stdout)
 
 
 @pytest.mark.gpu
