@@ -86,6 +86,9 @@ def parse():
     ap.add_argument("--link", action="store_true",
                     help="measure the CPU-GPU link: DMA copies between pinned host memory and HBM, and exit")
     ap.add_argument("--profile-first-tier", type=int, default=-1)
+    ap.add_argument("--profile-host-inputs", action="store_true",
+                    help="profiling case: the ASCII and descriptors in pinned host memory, read by the "
+                         "kernels in place over the CPU-GPU link (as wfe_align does with pinned buffers)")
     return ap.parse_args()
 
 
@@ -161,12 +164,16 @@ def run_profile_case(args) -> int:
     torch.cuda.set_device(0)
     n = args.profile_batch
     ascii, pairs = wfe.generate(n, LENGTH, p_min=EDIT_P, seed=SEED)
-    d_ascii = torch.from_numpy(ascii).cuda()
-    d_pairs = torch.from_numpy(pairs.view(np.uint8)).cuda()
+    if args.profile_host_inputs:
+        d_ascii = torch.from_numpy(ascii).pin_memory()
+        d_pairs = torch.from_numpy(pairs.view(np.uint8)).pin_memory()
+    else:
+        d_ascii = torch.from_numpy(ascii).cuda()
+        d_pairs = torch.from_numpy(pairs.view(np.uint8)).cuda()
     d_dist = torch.zeros(n, dtype=torch.int32, device="cuda")
     d_cigar = torch.zeros(n * CIGAR_STRIDE, dtype=torch.int8, device="cuda")
     d_status = torch.zeros(n, dtype=torch.uint8, device="cuda")
-    out = {"profile_batch": n, "kernel": args.profile_kernel}
+    out = {"profile_batch": n, "kernel": args.profile_kernel, "host_inputs": bool(args.profile_host_inputs)}
     with wfe.Context(max_seq_len=MAX_SEQ_LEN, batch_size=n, cigar_stride=CIGAR_STRIDE) as ctx:
         if args.profile_kernel == "tier":
             if args.profile_first_tier >= 0:
