@@ -555,6 +555,32 @@ def pageable_e2e(ascii, pairs, reps, local, world, device, want_dist) -> dict:
     return out
 
 
+def link_roofline(achieved_bps: float) -> dict:
+    """The e2e leg's bytes from host memory per second against the host-to-
+    device DMA rate of the CPU-GPU link measured here (256 MiB from pinned
+    memory, best of 3, CUDA events)."""
+    import torch
+    n = 256 << 20
+    h = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+    h.fill_(1)
+    d = torch.empty(n, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.Stream()
+    best = 1e9
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        with torch.cuda.stream(s):
+            d.copy_(h, non_blocking=True)
+        e1.record(s)
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    peak = n / (best * 1e-3) / 1e9
+    achieved = achieved_bps / 1e9
+    return {"bound": "CPU-GPU link (NVLink-C2C), host to device", "achieved": achieved, "peak": peak,
+            "unit": "GB/s", "frac": achieved / peak,
+            "peak_kind": "measured: 256 MiB DMA from pinned memory in this run"}
+
+
 def cigar_lengths(cg: np.ndarray) -> np.ndarray:
     """Bytes of each encoded CIGAR before its terminator."""
     z = cg == 0
@@ -806,6 +832,7 @@ def main():
     if not (np.array_equal(h_dist, d_dist.cpu().numpy())):
         raise SystemExit("host-buffer and device-buffer results differ")
     e2e["pageable"] = pageable_e2e(ascii, pairs, reps, local, world, device, h_dist)
+    e2e["link_roofline"] = link_roofline(h2d * reps * nb / e2e_s)
 
     base = None
     ref_cuda = None
