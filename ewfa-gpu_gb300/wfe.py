@@ -345,9 +345,15 @@ class Context:
         """Host buffers in, host buffers out: (dist int32[n], cigar int8[n, stride], status uint8[n])."""
         n = len(pairs)
         pairs = np.ascontiguousarray(pairs, dtype=PAIR_DTYPE)
+        ascii = np.ascontiguousarray(ascii)
         if out is None:
             out = (np.zeros(n, np.int32), np.zeros((n, self.cigar_stride), np.int8), np.zeros(n, np.uint8))
         dist, cg, st = out
+        # the library writes through raw pointers: outputs must be whole, contiguous arrays
+        for a, dt, size in ((dist, np.int32, n), (cg, np.int8, n * self.cigar_stride), (st, np.uint8, n)):
+            if a.dtype != dt or a.size != size or not a.flags.c_contiguous or not a.flags.writeable:
+                raise ValueError(f"output must be a writable C-contiguous {np.dtype(dt).name} array of {size} "
+                                 f"elements (got {a.dtype}, {a.size}, contiguous={a.flags.c_contiguous})")
         _check(load().wfe_align(self._h, _addr(ascii), ascii.nbytes, _addr(pairs), n, _addr(dist),
                                 _addr(cg), _addr(st)), "wfe_align")
         return dist, cg, st

@@ -159,3 +159,23 @@ def test_constants_match_the_header():
         assert getattr(wfe, name) == val, name
         checked += 1
     assert checked >= 22 and found["FLAG_PAGEABLE_IN_PLACE"] == 8
+
+
+def test_align_rejects_unusable_output_arrays():
+    """The Python binding checks the output arrays before the library writes
+    through their pointers (no device needed: the check comes first)."""
+    import types
+    ctx = types.SimpleNamespace(cigar_stride=8, _h=None)
+    ascii, pairs = wfe.pairs_from_list([(b"ACGT", b"ACGA")] * 3)
+    good = (np.zeros(3, np.int32), np.zeros((3, 8), np.int8), np.zeros(3, np.uint8))
+    bad_cases = [
+        (np.zeros(3, np.int64), good[1], good[2]),              # wrong dtype
+        (good[0], np.zeros((3, 16), np.int8)[:, ::2], good[2]),  # not contiguous
+        (good[0], good[1], np.zeros(2, np.uint8)),              # too short
+    ]
+    ro = np.zeros(3, np.int32)
+    ro.flags.writeable = False
+    bad_cases.append((ro, good[1], good[2]))                    # read-only
+    for out in bad_cases:
+        with pytest.raises(ValueError):
+            wfe.Context.align(ctx, ascii, pairs, out=out)
