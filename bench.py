@@ -86,6 +86,11 @@ def parse():
     ap.add_argument("--link", action="store_true",
                     help="measure the CPU-GPU link: DMA copies between pinned host memory and HBM, and exit")
     ap.add_argument("--profile-first-tier", type=int, default=-1)
+    ap.add_argument("--profile-case", choices=["workload"] + sorted(PROFILE_CASES), default="workload",
+                    help="profiling case: the --workload's pairs, or pairs for the CTA-per-pair tiers: "
+                         "deep (5,000-7,000 bases, p 0.06-0.10, distances of hundreds: tier 5's regime in the "
+                         "mixed workload), far (4,000-5,000 bases, p 0.70-0.80, distances around 2,000 and "
+                         "beyond: tier 6's)")
     ap.add_argument("--profile-host-inputs", action="store_true",
                     help="profiling case: the ASCII and descriptors in pinned host memory, read by the "
                          "kernels in place over the CPU-GPU link (as wfe_align does with pinned buffers)")
@@ -153,6 +158,15 @@ def histories_from_cigars(cg: np.ndarray) -> np.ndarray:
     return words
 
 
+# Profiling cases for the CTA-per-pair tiers: lengths (log-uniform), edit
+# probability (uniform), seed, max_seq_len, CIGAR stride, and the slab bounds
+# of tiers 5 and 6 (a few GB on the device in all).
+PROFILE_CASES = {
+    "deep": (5000, 7000, 0.06, 0.10, 44, 7400, 4096, (2 << 30, 1 << 30)),
+    "far": (4000, 5000, 0.70, 0.80, 46, 5200, 12000, (1 << 30, 2 << 30)),
+}
+
+
 def run_profile_case(args) -> int:
     """Profiling cases: every kernel runs twice over one batch of n pairs of
     the workload (the first launch warms up, ncu captures the second):
@@ -163,7 +177,12 @@ def run_profile_case(args) -> int:
     import torch
     torch.cuda.set_device(0)
     n = args.profile_batch
-    ascii, pairs = wfe.generate(n, LENGTH, p_min=EDIT_P, seed=SEED)
+    max_seq_len, stride, scratch = MAX_SEQ_LEN, CIGAR_STRIDE, None
+    if args.profile_case == "workload":
+        ascii, pairs = wfe.generate(n, LENGTH, p_min=EDIT_P, seed=SEED)
+    else:
+        lmin, lmax, pmin, pmax, seed, max_seq_len, stride, scratch = PROFILE_CASES[args.profile_case]
+        ascii, pairs = wfe.generate(n, lmin, lmax, p_min=pmin, p_max=pmax, seed=seed)
     if args.profile_host_inputs:
         d_ascii = torch.from_numpy(ascii).pin_memory()
         d_pairs = torch.from_numpy(pairs.view(np.uint8)).pin_memory()
@@ -171,19 +190,25 @@ def run_profile_case(args) -> int:
         d_ascii = torch.from_numpy(ascii).cuda()
         d_pairs = torch.from_numpy(pairs.view(np.uint8)).cuda()
     d_dist = torch.zeros(n, dtype=torch.int32, device="cuda")
-    d_cigar = torch.zeros(n * CIGAR_STRIDE, dtype=torch.int8, device="cuda")
+    d_cigar = torch.zeros(n * stride, dtype=torch.int8, device="cuda")
     d_status = torch.zeros(n, dtype=torch.uint8, device="cuda")
-    out = {"profile_batch": n, "kernel": args.profile_kernel, "host_inputs": bool(args.profile_host_inputs)}
-    with wfe.Context(max_seq_len=MAX_SEQ_LEN, batch_size=n, cigar_stride=CIGAR_STRIDE) as ctx:
+    out = {"profile_batch": n, "kernel": args.profile_kernel, "case": args.profile_case,
+           "host_inputs": bool(args.profile_host_inputs)}
+    with wfe.Context(max_seq_len=max_seq_len, batch_size=n, cigar_stride=stride, long_scratch=scratch) as ctx:
         if args.profile_kernel == "tier":
             if args.profile_first_tier >= 0:
-                ctx.set_policy([MAX_SEQ_LEN], [args.profile_first_tier])
+                ctx.set_policy([max_seq_len], [args.profile_first_tier])
             for _ in range(2):
-                ctx.align_device(d_ascii, d_pairs, n, MAX_SEQ_LEN, d_dist, d_cigar, d_status)
+                ctx.align_device(d_ascii, d_pairs, n, max_seq_len, d_dist, d_cigar, d_status)
                 torch.cuda.synchronize()
             out["tier_launches"] = ctx.stats()["tier_launches"][:7]
             out["tier_passed"] = ctx.stats()["tier_passed"][:7]
+            dist = d_dist.cpu().numpy().astype(np.float64)
+            out["distance"] = {"mean": float(dist.mean()), "max": float(dist.max()),
+                               "cells_per_pair": float(np.mean(dist * dist + 2 * dist))}
         else:
+            if args.profile_case != "workload":
+                raise SystemExit("--profile-kernel aux runs on the --workload's pairs")
             wps = (MAX_SEQ_LEN + 15) // 16
             d_words = torch.zeros(2 * n * wps, dtype=torch.int32, device="cuda")
             for _ in range(2):
@@ -201,7 +226,7 @@ def run_profile_case(args) -> int:
                                               CIGAR_STRIDE, d_st2)
             torch.cuda.synchronize()
             out["history_cigars_equal"] = bool(torch.equal(d_cg2, d_cigar))
-    mb = (len(ascii) + n * (CIGAR_STRIDE + 29)) / 2**20
+    mb = (len(ascii) + n * (stride + 29)) / 2**20
     out.update({"device_MiB": round(mb, 1), "status_ok": bool((d_status.cpu().numpy() == 0).all())})
     print(json.dumps(out))
     return 0

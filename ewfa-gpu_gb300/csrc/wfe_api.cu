@@ -469,6 +469,11 @@ extern "C" {
 
 int wfe_create(const wfe_config* cfg, wfe_ctx** out) { return wfe::create_context(cfg, 0, 0, out); }
 
+int wfe_create_with_scratch(const wfe_config* cfg, uint64_t tier5_bytes, uint64_t tier6_bytes, wfe_ctx** out)
+{
+    return wfe::create_context(cfg, tier5_bytes, tier6_bytes, out);
+}
+
 int wfe_set_policy(wfe_ctx* ctx, uint32_t nbuckets, const uint32_t* bucket_max_len, const int32_t* first_tier,
                    uint32_t flags)
 {

@@ -33,7 +33,7 @@ PAIR_DTYPE = np.dtype([("p_off", "<u8"), ("t_off", "<u8"), ("p_len", "<u4"), ("t
 assert PAIR_DTYPE.itemsize == 24
 
 SYMBOLS = [
-    "wfe_create", "wfe_destroy", "wfe_strerror", "wfe_last_cuda_error", "wfe_get_stats",
+    "wfe_create", "wfe_create_with_scratch", "wfe_destroy", "wfe_strerror", "wfe_last_cuda_error", "wfe_get_stats",
     "wfe_reset_stats", "wfe_align", "wfe_align_strided", "wfe_align_device", "wfe_pack_device",
     "wfe_cigar_from_history_device", "wfe_format_cigar", "wfe_check_cigar", "wfe_align_device_noalloc",
     "wfe_read_pair_file", "wfe_free_pair_file", "wfe_host_alloc", "wfe_host_free", "wfe_device_count",
@@ -108,6 +108,7 @@ def load() -> C.CDLL:
     L = C.CDLL(LIB_PATH)
     vp, sz, u32, i32 = C.c_void_p, C.c_size_t, C.c_uint32, C.c_int32
     L.wfe_create.argtypes = [C.POINTER(Config), C.POINTER(C.c_void_p)]
+    L.wfe_create_with_scratch.argtypes = [C.POINTER(Config), C.c_uint64, C.c_uint64, C.POINTER(C.c_void_p)]
     L.wfe_destroy.argtypes = [vp]
     L.wfe_destroy.restype = None
     L.wfe_strerror.argtypes = [C.c_int]
@@ -266,14 +267,22 @@ class Context:
     place on a GB300 (the GPU reads the CPU's page tables): 1M x 150-base
     pairs with fresh output arrays take ~4 ms instead of ~29 ms staged.  Bad
     descriptors are then reported per pair, as with pinned arrays, instead
-    of failing the call."""
+    of failing the call.
+
+    long_scratch=(tier5_bytes, tier6_bytes) bounds the device memory of the
+    CTA-per-pair tiers' slabs (wfe_create_with_scratch); None keeps the
+    defaults."""
 
     def __init__(self, max_seq_len: int, batch_size: int = 100000, max_distance: int = 0,
-                 cigar_stride: int = 0, device: int = 0, flags: int = 0):
+                 cigar_stride: int = 0, device: int = 0, flags: int = 0, long_scratch=None):
         L = load()
         self.cfg = Config(device, max_seq_len, batch_size, max_distance, cigar_stride, flags)
         h = C.c_void_p()
-        rc = L.wfe_create(C.byref(self.cfg), C.byref(h))
+        if long_scratch is None:
+            rc = L.wfe_create(C.byref(self.cfg), C.byref(h))
+        else:
+            b5, b6 = long_scratch
+            rc = L.wfe_create_with_scratch(C.byref(self.cfg), int(b5), int(b6), C.byref(h))
         if rc != OK:
             raise WfeError(rc, f"wfe_create (cuda error {L.wfe_last_cuda_error(None)})")
         self._h = h

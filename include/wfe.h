@@ -137,6 +137,16 @@ typedef struct wfe_stats {
  * cudaSetDevice does, src/aligner.cu:147). */
 int wfe_create(const wfe_config* cfg, wfe_ctx** out);
 
+/* wfe_create with a bound on the device memory of the CTA-per-pair tiers'
+ * slabs: one slab per resident CTA holds a pair's backtrace store, operation
+ * chain and runs (tier 6: also its wavefront).  tier5_bytes and tier6_bytes
+ * bound tiers 5 and 6; 0 keeps wfe_create's 2 GiB and 8 GiB.  A smaller
+ * bound lowers only how many pairs those tiers align at once (never fewer
+ * than one); the results are the same.  No reference counterpart: the
+ * reference has neither tier (its distance search stops at 63). */
+int wfe_create_with_scratch(const wfe_config* cfg, uint64_t tier5_bytes, uint64_t tier6_bytes,
+                            wfe_ctx** out);
+
 /* Release everything the context owns.  Replaces GPU_memory_free
  * (src/wavefront.cu:110-125). */
 void wfe_destroy(wfe_ctx* ctx);

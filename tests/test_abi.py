@@ -52,6 +52,9 @@ def test_create_without_device_fails_cleanly():
     with pytest.raises(wfe.WfeError) as e:
         wfe.Context(max_seq_len=150)
     assert e.value.code == wfe.ERR_NO_DEVICE
+    with pytest.raises(wfe.WfeError) as e:
+        wfe.Context(max_seq_len=150, long_scratch=(1 << 20, 1 << 20))
+    assert e.value.code == wfe.ERR_NO_DEVICE
 
 
 def test_create_rejects_bad_config():
@@ -59,6 +62,7 @@ def test_create_rejects_bad_config():
     cfg = wfe.Config(0, 0, 0, 0, 0, 0)
     h = C.c_void_p()
     assert wfe.load().wfe_create(C.byref(cfg), C.byref(h)) == wfe.ERR_INVALID_ARGUMENT
+    assert wfe.load().wfe_create_with_scratch(C.byref(cfg), 1 << 20, 1 << 20, C.byref(h)) == wfe.ERR_INVALID_ARGUMENT
 
 
 def test_format_and_check_match_oracle_on_golden():

@@ -519,10 +519,9 @@ def test_pinned_strided_layout():
     compare_with_oracle(ascii, pairs, 152, *want)
 
 
-def test_long_tiers_without_distance_limit():
-    """Unrelated random pairs (distance about half the length) reach the
-    CTA-per-pair tiers: shared-memory wavefront up to distance 2047 (tier
-    5), global-memory wavefront beyond (tier 6)."""
+def _long_tier_pairs():
+    """Unrelated random pairs (distance about half the length) and a few
+    near-identical long ones."""
     rng = np.random.default_rng(5)
     seqs = []
     def rand(L):
@@ -537,7 +536,13 @@ def test_long_tiers_without_distance_limit():
         for j in rng.choice(L, 40, replace=False):
             p[j] = b"ACGT"[(b"ACGT".index(p[j]) + 1) % 4]
         seqs.append((bytes(p), t))
-    ascii, pairs = wfe.pairs_from_list(seqs)
+    return wfe.pairs_from_list(seqs)
+
+
+def test_long_tiers_without_distance_limit():
+    """The pairs reach the CTA-per-pair tiers: shared-memory wavefront up to
+    distance 2047 (tier 5), global-memory wavefront beyond (tier 6)."""
+    ascii, pairs = _long_tier_pairs()
     with wfe.Context(max_seq_len=5000, cigar_stride=12000) as ctx:
         dist, cg, st = ctx.align(ascii, pairs)
         stats = ctx.stats()
@@ -545,6 +550,22 @@ def test_long_tiers_without_distance_limit():
     assert stats["tier_passed"][4] > 0 and stats["tier_passed"][5] > 0, stats
     assert (st == 0).all()
     compare_with_oracle(ascii, pairs, 12000, dist, cg, st)
+
+
+def test_long_tiers_in_one_slab_each():
+    """wfe_create_with_scratch with bounds below one slab: tiers 5 and 6 each
+    align one pair at a time, with the same results."""
+    torch_cuda()
+    ascii, pairs = _long_tier_pairs()
+    with wfe.Context(max_seq_len=5000, cigar_stride=12000) as ctx:
+        want = ctx.align(ascii, pairs)
+    with wfe.Context(max_seq_len=5000, cigar_stride=12000, long_scratch=(1, 1)) as ctx:
+        got = ctx.align(ascii, pairs)
+        stats = ctx.stats()
+    assert stats["tier_passed"][4] > 0 and stats["tier_passed"][5] > 0, stats
+    np.testing.assert_array_equal(got[0], want[0])
+    np.testing.assert_array_equal(got[2], want[2])
+    assert_same_cigars(got[1], want[1])
 
 
 @pytest.mark.parametrize("first_tier", [5, 6])
