@@ -288,7 +288,11 @@ __device__ __forceinline__ int extend_lane(const uint2* QP, const uint2* QT,
 /* The same longest common prefix computed by a group of G lanes at once:
  * lane g compares the window 16*g bases further on, a ballot finds the first
  * window that is not a full match.  Returns the run length.  All lanes of
- * the group call with the same arguments. */
+ * the group call with the same arguments.
+ * A warp-wide group (G = 32, one pair per warp) first compares the first
+ * window on every lane -- the same shared-memory words, so one broadcast
+ * read -- and a run shorter than 16 bases, the common case at high error
+ * rates, is then known on every lane without the vote and shuffle. */
 template <int G>
 __device__ __forceinline__ int group_extend(const uint2* QP, const uint2* QT, int plen,
                                             int tlen, int k, int off, int g, int grp,
@@ -296,6 +300,15 @@ __device__ __forceinline__ int group_extend(const uint2* QP, const uint2* QT, in
 {
     const int v0 = off - k, h0 = off;
     int total = 0;
+    if constexpr (G == 32) {
+        int n = 0;
+        if ((unsigned)v0 < (unsigned)plen && (unsigned)h0 < (unsigned)tlen) {
+            const uint32_t x = window(QP, v0) ^ window(QT, h0);
+            n = min(__clz(x) >> 1, min(plen - v0, tlen - h0));
+        }
+        if (n < 16) return n;
+        total = 16;
+    }
     for (;;) {
         const int v = v0 + total + 16 * g, h = h0 + total + 16 * g;
         int n = 0;
