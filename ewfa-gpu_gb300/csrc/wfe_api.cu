@@ -183,7 +183,7 @@ void plan_bucket(wfe_ctx* ctx, BucketPlan& b)
     b.last_tier = b.max_len > (uint32_t)kLongSmemDistance ? 6 : 5;
     for (int t = 0; t < kNumTiers; ++t) {
         TierShape sh = tier_shape(t, b.max_len, c.cigar_stride, ctx->sm_count);
-        if (t >= 3 && sh.grid > 0) sh.grid = std::min(sh.grid, ctx->scratch_ctas[t]);
+        if (t >= 2 && sh.grid > 0) sh.grid = std::min(sh.grid, ctx->scratch_ctas[t]);
         if (t >= 5 && sh.grid > 0) {
             sh.slab = ctx->long_slab[t];
             sh.scratch = ctx->d_long_scratch[t];
@@ -414,7 +414,7 @@ int create_context(const wfe_config* cfg, uint64_t budget5, uint64_t budget6, wf
     for (int t = 0; t <= last; ++t) {
         const TierShape sh = tier_shape(t, c.max_seq_len, c.cigar_stride, ctx->sm_count);
         if (sh.grid <= 0) continue;
-        if (t == 3 || t == 4) {
+        if (t >= 2 && t <= 4) {
             ctx->scratch_ctas[t] = sh.grid;
             scratch = std::max(scratch, tier_scratch_bytes(t, sh.grid));
         } else if (t >= 5) {

@@ -105,8 +105,9 @@ struct Tier {
     using E = typename OE::T;
     /* Row d of the backtrace store.  The 32-lane tiers keep only the chunks
      * that score step d touches -- the contiguous range whose diagonals meet
-     * [-d, d] -- row after row (a triangle, 55-68 % of DCAP x NC entries):
-     * their store in shared memory is what limits their occupancy.  Tier 0
+     * [-d, d] -- row after row (a triangle, 55-68 % of DCAP x NC entries),
+     * which keeps tier 1's store in shared memory small and tiers 2-4's
+     * global scratch mostly in L2.  Tier 0
      * keeps full rows: its occupancy is set by registers, and it is
      * issue-bound, so it saves the index arithmetic instead. */
     static constexpr bool TRI = G == 32;
@@ -190,7 +191,7 @@ using T0 = Tier<4, WFE_T0_J, true, 5, WFE_T0_MINB>; /* distance <= 4*J + 1 (21) 
 template <bool GLOBAL_WF>
 __global__ void long_kernel(const __grid_constant__ AlignLaunch A);
 using T1 = Tier<32, 2, true, 1>;   /* distance <= 79  */
-using T2 = Tier<32, 4, true, 1>;   /* distance <= 143 */
+using T2 = Tier<32, 4, false, 1>;  /* distance <= 143; backtrace store in global scratch: 8 CTAs per SM */
 using T3 = Tier<32, 8, false, 1>;  /* distance <= 271 */
 using T4 = Tier<32, 16, false, 1>; /* distance <= 527 */
 
@@ -940,6 +941,7 @@ const TierInfo& tier_info(int t) { return kTiers[t]; }
 size_t tier_scratch_bytes(int tier, int grid)
 {
     switch (tier) {
+    case 2: return T2::ops_bytes * (size_t)grid * (kWarps * T2::GPW);
     case 3: return T3::ops_bytes * (size_t)grid * (kWarps * T3::GPW);
     case 4: return T4::ops_bytes * (size_t)grid * (kWarps * T4::GPW);
     default: return 0;
