@@ -768,15 +768,22 @@ def main():
                       flags=wfe.FLAG_KERNEL_TIMING)
     pair_bytes = wfe.PAIR_DTYPE.itemsize
 
-    def step(i):
-        b = i % nb
-        ctx.align_device(d_ascii, d_pairs.data_ptr() + b * BATCH * pair_bytes, BATCH, MAX_SEQ_LEN,
-                         d_dist.data_ptr() + 4 * b * BATCH, d_cigar.data_ptr() + b * BATCH * CIGAR_STRIDE,
-                         d_status.data_ptr() + b * BATCH, stream)
+    def steps(first, count):
+        """Steps first .. first+count-1 (step i aligns batch i mod nb): one
+        wfe_align_device call per run of consecutive batches, so that the
+        library overlaps each batch's last CTAs with the next batch's first,
+        as a caller aligning many device-resident batches at once does."""
+        i = first
+        while i < first + count:
+            b = i % nb
+            k = min(nb - b, first + count - i)
+            ctx.align_device(d_ascii, d_pairs.data_ptr() + b * BATCH * pair_bytes, k * BATCH, MAX_SEQ_LEN,
+                             d_dist.data_ptr() + 4 * b * BATCH, d_cigar.data_ptr() + b * BATCH * CIGAR_STRIDE,
+                             d_status.data_ptr() + b * BATCH, stream)
+            i += k
 
     with torch.cuda.stream(stream):
-        for i in range(max(3, args.warmup)):
-            step(i)
+        steps(0, max(3, args.warmup))
     torch.cuda.synchronize()
     ctx.reset_stats()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -784,8 +791,7 @@ def main():
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
         start.record(stream)
-        for i in range(args.steps):
-            step(i)
+        steps(0, args.steps)
         end.record(stream)
         torch.cuda.synchronize()
     barrier(world, device)

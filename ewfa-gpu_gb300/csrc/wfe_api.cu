@@ -86,7 +86,7 @@ struct wfe_ctx {
     BucketPlan bucket[kMaxBuckets];
     bool predict = false;                      /* route pairs by predicted distance */
     int scratch_ctas[kNumTiers] = {};          /* CTAs whose global scratch is allocated */
-    unsigned char* d_ops_scratch = nullptr;    /* tiers 3-4 backtrace stores */
+    unsigned char* d_ops_scratch = nullptr;    /* tiers 2-4 backtrace stores */
     size_t ops_scratch_bytes = 0;
     unsigned char* d_long_scratch[kNumTiers] = {}; /* tiers 5-6 slabs */
     uint64_t long_slab[kNumTiers] = {};
@@ -101,6 +101,8 @@ struct wfe_ctx {
     wfe_stats stats{};
     std::vector<TimedLaunch> timed;            /* launches whose events are not read yet */
     std::vector<cudaEvent_t> event_pool;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr; /* device calls of several batches: stage 1's stream
+                                                         after the caller's, and back */
 };
 
 namespace {
@@ -465,6 +467,10 @@ int create_context(const wfe_config* cfg, uint64_t budget5, uint64_t budget6, wf
 
 }  // namespace wfe
 
+namespace {
+int ensure_stage_scratch(wfe_ctx* ctx, Stage& s);
+}  // namespace
+
 extern "C" {
 
 int wfe_create(const wfe_config* cfg, wfe_ctx** out) { return wfe::create_context(cfg, 0, 0, out); }
@@ -530,6 +536,8 @@ void wfe_destroy(wfe_ctx* ctx)
         cudaEventDestroy(t.stop);
     }
     for (auto ev : ctx->event_pool) cudaEventDestroy(ev);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     delete ctx;
 }
 
@@ -584,20 +592,42 @@ int wfe_align_device(wfe_ctx* ctx, const char* d_ascii, const wfe_pair* d_pairs,
     if (const int r = pop_launch_error(ctx)) return r;
     cudaStream_t s = stream ? (cudaStream_t)stream : ctx->st[0].stream;
     const size_t B = ctx->cfg.batch_size;
-    for (size_t b0 = 0; b0 < n; b0 += B) {
+    /* Several batches alternate between `stream` (stage 0) and stage 1's
+     * stream, which first waits for the work already on `stream` and which
+     * `stream` waits for at the end: the last CTAs of one batch then share
+     * the GPU with the first of the next, and the call stays ordered on
+     * `stream`.  Stage 1 has its own work lists and tier scratch (allocated
+     * by the first call that needs them); without them the batches run one
+     * after another. */
+    int nstages = 1;
+    if (n > B && !(ctx->cfg.flags & WFE_FLAG_NO_PIPELINE) && ensure_stage_scratch(ctx, ctx->st[1]) == WFE_OK) {
+        if (!ctx->ev_fork) WFE_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+        if (!ctx->ev_join) WFE_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+        WFE_CUDA(ctx, cudaEventRecord(ctx->ev_fork, s));
+        WFE_CUDA(ctx, cudaStreamWaitEvent(ctx->st[1].stream, ctx->ev_fork, 0));
+        nstages = 2;
+    }
+    int rc = WFE_OK;
+    size_t bi = 0;
+    for (size_t b0 = 0; b0 < n && rc == WFE_OK; b0 += B, ++bi) {
         const uint32_t nb = (uint32_t)std::min(B, n - b0);
+        const int si = (int)(bi % (size_t)nstages);
         Layout L{};
         L.ascii = d_ascii;
         L.pairs = d_pairs + b0;
         L.base_off = 0;
-        const int r = run_chain(ctx, ctx->st[0], L, nb, d_dist + b0,
-                                d_cigar ? d_cigar + b0 * ctx->cfg.cigar_stride : nullptr,
-                                d_status ? d_status + b0 : nullptr, s);
-        if (r != WFE_OK) return r;
+        rc = run_chain(ctx, ctx->st[si], L, nb, d_dist + b0, d_cigar ? d_cigar + b0 * ctx->cfg.cigar_stride : nullptr,
+                       d_status ? d_status + b0 : nullptr, si ? ctx->st[1].stream : s);
+        if (rc != WFE_OK) break;
         ctx->stats.batches++;
         ctx->stats.pairs += nb;
     }
-    return WFE_OK;
+    if (nstages == 2) {
+        /* also after a failed enqueue: nothing on `stream` may overtake stage 1 */
+        WFE_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->st[1].stream));
+        WFE_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_join, 0));
+    }
+    return rc;
 }
 
 }  // extern "C"

@@ -90,7 +90,8 @@ typedef struct wfe_config {
     uint32_t flags;        /* WFE_FLAG_* */
 } wfe_config;
 
-#define WFE_FLAG_NO_PIPELINE 1u   /* host calls: one batch in flight (no copy/compute overlap) */
+#define WFE_FLAG_NO_PIPELINE 1u   /* one batch in flight: no copy/compute overlap in host
+                                     calls, no second stream in device calls */
 #define WFE_FLAG_KERNEL_TIMING 2u /* time every kernel launch with CUDA events on its
                                      stream; read back by wfe_get_stats */
 #define WFE_FLAG_DEVICE_ONLY 4u   /* no staging buffers for host calls: the context
@@ -258,6 +259,13 @@ int wfe_align_strided(wfe_ctx* ctx, const char* ascii, size_t stride,
  * wfe_align_strided report it themselves.  The device calls of a context
  * share its work lists and scratch: enqueue them on one stream (or order
  * them), and synchronise that stream before a host call on the context.
+ * A call of more than batch_size pairs runs its batches on two streams --
+ * `stream` and one of the context's -- so that consecutive batches overlap
+ * on the device; the context's stream waits for the work already on
+ * `stream`, and `stream` waits for it at the end, so the call stays ordered
+ * on `stream`.  The first such call allocates the second stream's tier
+ * scratch (about as much as wfe_create did; without it the batches run one
+ * after another; WFE_FLAG_NO_PIPELINE keeps them on `stream` alone).
  * Replaces the kernel chain WF_edit_distance -> generate_cigars
  * (src/wavefront.cu:203-260). */
 int wfe_align_device(wfe_ctx* ctx, const char* d_ascii,

@@ -237,6 +237,40 @@ def test_two_stages_in_the_scratch_tiers():
     compare_with_oracle(ascii, pairs, 3000, d1, c1, s1)
 
 
+def test_device_call_of_several_batches_on_two_streams():
+    """wfe_align_device over more than batch_size pairs alternates its
+    batches between the caller's stream and a stream of the context, each
+    with its own scratch of tiers 2-6.  Results equal one-stream calls
+    (FLAG_NO_PIPELINE) and the oracle's, and work enqueued on the caller's
+    stream after the call sees every batch's results."""
+    torch = torch_cuda()
+    ascii, pairs = wfe.generate(3000, 300, 2600, p_min=0.2, p_max=0.45, seed=43)
+    n, stride = len(pairs), 3000
+    d_ascii = torch.from_numpy(ascii).cuda()
+    d_pairs = torch.from_numpy(pairs.view(np.uint8)).cuda()
+    out = {}
+    for flags in (0, wfe.FLAG_NO_PIPELINE):
+        d_dist = torch.full((n,), -7, dtype=torch.int32, device="cuda")
+        d_cg = torch.zeros(n * stride, dtype=torch.int8, device="cuda")
+        d_st = torch.full((n,), 255, dtype=torch.uint8, device="cuda")
+        s = torch.cuda.Stream()
+        with wfe.Context(max_seq_len=2700, batch_size=150, cigar_stride=stride, flags=flags) as ctx:
+            for _ in range(2):
+                ctx.align_device(d_ascii, d_pairs, n, 2700, d_dist, d_cg, d_st, s)
+                with torch.cuda.stream(s):
+                    # runs after the call on the same stream: must see all of it
+                    unset = int((d_st == 255).sum().item())
+                assert unset == 0
+            st = ctx.stats()
+        assert st["batches"] == 40 and st["tier_passed"][3] > 0 and st["tier_passed"][4] > 0, st
+        out[flags] = (d_dist.cpu().numpy(), d_cg.view(n, stride).cpu().numpy(), d_st.cpu().numpy())
+    a, b = out[0], out[wfe.FLAG_NO_PIPELINE]
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[2], b[2])
+    assert_same_cigars(a[1], b[1])
+    compare_with_oracle(ascii, pairs, stride, *a)
+
+
 def test_warp_span_layouts():
     """Tier 0 loads a warp's 8 pairs as one coalesced span when they lie
     within 2,560 bytes.  Layouts that exercise it: each warp's 16 sequences
