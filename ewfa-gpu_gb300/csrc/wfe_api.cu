@@ -600,12 +600,17 @@ int wfe_align_device(wfe_ctx* ctx, const char* d_ascii, const wfe_pair* d_pairs,
      * by the first call that needs them); without them the batches run one
      * after another. */
     int nstages = 1;
-    if (n > B && !(ctx->cfg.flags & WFE_FLAG_NO_PIPELINE) && ensure_stage_scratch(ctx, ctx->st[1]) == WFE_OK) {
-        if (!ctx->ev_fork) WFE_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
-        if (!ctx->ev_join) WFE_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
-        WFE_CUDA(ctx, cudaEventRecord(ctx->ev_fork, s));
-        WFE_CUDA(ctx, cudaStreamWaitEvent(ctx->st[1].stream, ctx->ev_fork, 0));
-        nstages = 2;
+    if (n > B && !(ctx->cfg.flags & WFE_FLAG_NO_PIPELINE)) {
+        const int seen = ctx->last_cuda_error;
+        if (ensure_stage_scratch(ctx, ctx->st[1]) == WFE_OK) {
+            if (!ctx->ev_fork) WFE_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+            if (!ctx->ev_join) WFE_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+            WFE_CUDA(ctx, cudaEventRecord(ctx->ev_fork, s));
+            WFE_CUDA(ctx, cudaStreamWaitEvent(ctx->st[1].stream, ctx->ev_fork, 0));
+            nstages = 2;
+        } else {
+            ctx->last_cuda_error = seen; /* no failure of the call: its batches run on `stream` alone */
+        }
     }
     int rc = WFE_OK;
     size_t bi = 0;
