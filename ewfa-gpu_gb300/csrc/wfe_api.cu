@@ -51,7 +51,7 @@ struct Stage {
     uint16_t* d_pred = nullptr;   /* predicted prefix distances */
     char* h_stage = nullptr;      /* pinned gather buffer for scattered inputs */
     wfe_pair* h_pairs = nullptr;  /* pinned descriptors of a gathered batch */
-    /* Scratch of tiers 3-6 owned by this stage (stage 1 only; stage 0 uses
+    /* Scratch of tiers 2-6 owned by this stage (stage 1 only; stage 0 uses
      * the context's): the chains of the two stages run at the same time, and
      * a tier's CTAs index their scratch by blockIdx, so two grids of one tier
      * must not share it. */
@@ -836,7 +836,7 @@ int ensure_staging(wfe_ctx* ctx, Stage& s)
     return fail_cuda(ctx, e);
 }
 
-/* Stage 1's own scratch of tiers 3-6, the size of the context's, allocated
+/* Stage 1's own scratch of tiers 2-6, the size of the context's, allocated
  * when a host call first runs two batches at once.  A failed allocation
  * leaves none of it behind. */
 int ensure_stage_scratch(wfe_ctx* ctx, Stage& s)
