@@ -105,8 +105,8 @@ double now_s()
 
 struct Share {
     size_t first = 0, n = 0;
-    /* left uninitialised: libwfe makes the pages present (in parallel)
-     * and the kernels write them in place */
+    /* never initialised: helper threads only make the pages present, and
+     * the kernels write the results in place */
     std::unique_ptr<int32_t[]> dist;
     std::unique_ptr<int8_t[]> cigar;
     std::unique_ptr<uint8_t[]> status;
@@ -221,6 +221,32 @@ int main(int argc, char** argv)
             b = sh.n;
         }
         if (sh.n == 0) return;
+        /* Results that are printed or checked are kept for the whole share.
+         * Otherwise, as the reference keeps one batch of CIGARs on the host
+         * (src/wavefront.cu:267-300), a window of two batches (both
+         * pipeline stages busy) is written over and over.  The window's
+         * fresh pages are made present by four helper threads while the
+         * context is created: the kernels write them in place, and the first
+         * touch of a page (the kernel zeroing it) is the slow part. */
+        const size_t window = keep ? sh.n : std::min(sh.n, 2 * b);
+        sh.dist.reset(new int32_t[window]);
+        sh.cigar.reset(new int8_t[window * stride]);
+        sh.status.reset(new uint8_t[window]);
+        std::vector<std::thread> touch;
+        {
+            char* ranges[3] = {(char*)sh.dist.get(), (char*)sh.cigar.get(), (char*)sh.status.get()};
+            const size_t bytes[3] = {window * sizeof(int32_t), window * (size_t)stride, window};
+            constexpr unsigned kTouchThreads = 4;
+            for (unsigned k = 0; k < kTouchThreads; ++k)
+                touch.emplace_back([=] {
+                    const size_t page = 4096; /* every 4 KiB: covers any page size */
+                    for (int r = 0; r < 3; ++r) {
+                        const size_t lo = bytes[r] * k / kTouchThreads, hi = bytes[r] * (k + 1) / kTouchThreads;
+                        for (size_t i = lo; i < hi; i += page) ranges[r][i] = 0;
+                        if (hi > lo) ranges[r][hi - 1] = 0;
+                    }
+                });
+        }
         wfe_config cfg{};
         cfg.device = device;
         cfg.max_seq_len = max_len;
@@ -230,6 +256,7 @@ int main(int argc, char** argv)
         cfg.flags = WFE_FLAG_PAGEABLE_IN_PLACE; /* the results go straight to this share's arrays */
         wfe_ctx* ctx = nullptr;
         sh.rc = wfe_create(&cfg, &ctx);
+        for (auto& x : touch) x.join();
         if (sh.rc != WFE_OK) {
             sh.what = "wfe_create";
             return;
@@ -243,14 +270,6 @@ int main(int argc, char** argv)
             for (size_t i = 0; i < sh.n; ++i) mine[i] = *pair_at(sh.first + i);
             src = mine.data();
         }
-        /* Results that are printed or checked are kept for the whole share.
-         * Otherwise, as the reference keeps one batch of CIGARs on the host
-         * (src/wavefront.cu:267-300), a window of two batches (both
-         * pipeline stages busy) is written over and over. */
-        const size_t window = keep ? sh.n : std::min(sh.n, 2 * b);
-        sh.dist.reset(new int32_t[window]);
-        sh.cigar.reset(new int8_t[window * stride]);
-        sh.status.reset(new uint8_t[window]);
         for (size_t c0 = 0; c0 < sh.n && sh.rc == WFE_OK; c0 += window) {
             sh.rc = wfe_align(ctx, pf.ascii, pf.ascii_bytes, src + c0, std::min(window, sh.n - c0), sh.dist.get(),
                               sh.cigar.get(), sh.status.get());

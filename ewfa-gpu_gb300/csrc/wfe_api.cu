@@ -38,6 +38,9 @@ constexpr int kStages = 2;
 
 struct Stage {
     cudaStream_t stream = nullptr;
+    /* device buffers of host calls that stage, carved from one allocation
+     * (staging_arena) made by the first such call */
+    unsigned char* staging_arena = nullptr;
     char* d_ascii = nullptr;
     size_t ascii_cap = 0;
     wfe_pair* d_pairs = nullptr;
@@ -46,7 +49,8 @@ struct Stage {
     int32_t* d_dist = nullptr;
     int8_t* d_cigar = nullptr;
     uint8_t* d_status = nullptr;
-    uint32_t* d_lists = nullptr;  /* two retry lists of batch_size entries */
+    /* in the context's arena: */
+    uint32_t* d_lists = nullptr;  /* a work list of batch_size entries per bucket and tier */
     uint32_t* d_counts = nullptr; /* per bucket: list counts, finished CTAs, work counters */
     uint16_t* d_pred = nullptr;   /* predicted prefix distances */
     char* h_stage = nullptr;      /* pinned gather buffer for scattered inputs */
@@ -54,10 +58,24 @@ struct Stage {
     /* Scratch of tiers 2-6 owned by this stage (stage 1 only; stage 0 uses
      * the context's): the chains of the two stages run at the same time, and
      * a tier's CTAs index their scratch by blockIdx, so two grids of one tier
-     * must not share it. */
+     * must not share it.  One allocation, scratch_arena. */
+    unsigned char* scratch_arena = nullptr;
     unsigned char* own_ops_scratch = nullptr;
     unsigned char* own_long_scratch[kNumTiers] = {};
     bool own_scratch = false;
+};
+
+/* Sub-buffers carved from one device allocation, each 256-byte aligned: a
+ * cudaMalloc or cudaFree costs 40-140 us on this path whatever its size, so
+ * a context makes one at creation and frees one at teardown. */
+struct Carve {
+    size_t used = 0;
+    size_t take(size_t bytes)
+    {
+        const size_t at = used;
+        used += (bytes + 255u) & ~size_t(255);
+        return at;
+    }
 };
 
 thread_local int g_last_create_error = 0;
@@ -86,6 +104,11 @@ struct wfe_ctx {
     BucketPlan bucket[kMaxBuckets];
     bool predict = false;                      /* route pairs by predicted distance */
     int scratch_ctas[kNumTiers] = {};          /* CTAs whose global scratch is allocated */
+    unsigned char* d_arena = nullptr;          /* the one allocation holding the buffers below, both
+                                                  stages' work lists, counters and predictions and,
+                                                  for host calls, stage 1's own tier scratch */
+    int lists_buckets = 1;                     /* length buckets the stages' work lists have room for */
+    uint32_t* d_lists_ext = nullptr;           /* work lists of more buckets (wfe_set_policy) */
     unsigned char* d_ops_scratch = nullptr;    /* tiers 2-4 backtrace stores */
     size_t ops_scratch_bytes = 0;
     unsigned char* d_long_scratch[kNumTiers] = {}; /* tiers 5-6 slabs */
@@ -93,8 +116,10 @@ struct wfe_ctx {
     unsigned long long* d_passed = nullptr;    /* pairs each tier handed on, running total */
     unsigned long long* d_launched = nullptr;  /* tier launches made on the device */
     unsigned long long* d_bucket_total = nullptr; /* pairs classified into each bucket */
-    uint32_t* h_launch_error = nullptr;        /* host-mapped: bit t, a device-side launch of tier t failed */
-    uint32_t* d_launch_error = nullptr;        /* its device address */
+    uint8_t* h_launch_error = nullptr;         /* byte t: a device-side launch of tier t failed */
+    uint8_t* d_launch_error = nullptr;         /* its device address */
+    bool launch_error_pinned = false;          /* from cudaHostAlloc (else new[]: pageable memory the
+                                                  device reaches through the CPU's page tables) */
     uint64_t single_entered[kNumTiers] = {};   /* first-tier entries of one-bucket batches */
     Stage st[kStages];
     int last_cuda_error = 0;
@@ -128,10 +153,22 @@ int fail_cuda(wfe_ctx* ctx, cudaError_t e)
  * the work in question has completed. */
 int pop_launch_error(wfe_ctx* ctx)
 {
-    volatile uint32_t* f = ctx->h_launch_error;
+    volatile uint64_t* f = reinterpret_cast<volatile uint64_t*>(ctx->h_launch_error);
     if (!f || *f == 0u) return WFE_OK;
     *f = 0u;
     return fail_cuda(ctx, cudaErrorLaunchFailure);
+}
+
+constexpr size_t kLaunchErrorBytes = 8; /* one byte per tier (kNumTiers <= 8) */
+static_assert(kNumTiers <= (int)kLaunchErrorBytes, "one launch-error byte per tier");
+
+void free_launch_error(wfe_ctx* ctx)
+{
+    if (ctx->launch_error_pinned)
+        cudaFreeHost(ctx->h_launch_error);
+    else
+        delete[] reinterpret_cast<uint64_t*>(ctx->h_launch_error);
+    ctx->h_launch_error = ctx->d_launch_error = nullptr;
 }
 
 uint32_t default_cigar_stride(uint32_t max_seq_len)
@@ -155,24 +192,15 @@ int default_first_tier(uint32_t max_len)
  * tier */
 constexpr size_t kChainWords = 3 * kNumTiers + 1;
 constexpr size_t kCountWords = kMaxBuckets * kChainWords;
-constexpr size_t kLists = (size_t)kMaxBuckets * kNumTiers;
 
+/* What a stage owns itself: its staging and scratch allocations, pinned
+ * gather buffers and stream (its lists live in the context's arena). */
 void free_stage(Stage& s)
 {
-    cudaFree(s.d_ascii);
-    cudaFree(s.d_pairs);
-    cudaFree(s.d_plen);
-    cudaFree(s.d_tlen);
-    cudaFree(s.d_dist);
-    cudaFree(s.d_cigar);
-    cudaFree(s.d_status);
-    cudaFree(s.d_lists);
-    cudaFree(s.d_counts);
-    cudaFree(s.d_pred);
+    cudaFree(s.staging_arena);
+    cudaFree(s.scratch_arena);
     cudaFreeHost(s.h_stage);
     cudaFreeHost(s.h_pairs);
-    cudaFree(s.own_ops_scratch);
-    for (auto p : s.own_long_scratch) cudaFree(p);
     if (s.stream) cudaStreamDestroy(s.stream);
     s = Stage();
 }
@@ -394,10 +422,8 @@ int create_context(const wfe_config* cfg, uint64_t budget5, uint64_t budget6, wf
         g_last_create_error = (int)err;
         cudaGetLastError(); /* reported here, not to a later call */
         for (auto& s : ctx->st) free_stage(s);
-        cudaFree(ctx->d_ops_scratch);
-        cudaFree(ctx->d_passed);
-        cudaFreeHost(ctx->h_launch_error);
-        for (auto p : ctx->d_long_scratch) cudaFree(p);
+        cudaFree(ctx->d_arena);
+        free_launch_error(ctx);
         delete ctx;
         return err == cudaErrorMemoryAllocation ? WFE_ERR_OUT_OF_MEMORY : WFE_ERR_CUDA;
     };
@@ -410,15 +436,18 @@ int create_context(const wfe_config* cfg, uint64_t budget5, uint64_t budget6, wf
     ctx->host_page_tables = hpt != 0;
     /* Global scratch is sized for the longest sequences (max_seq_len); a
      * bucket of shorter sequences has more resident CTAs and uses at most
-     * the CTAs that scratch was sized for. */
+     * the CTAs that scratch was sized for.  Everything the context keeps on
+     * the device is carved from one allocation. */
     size_t scratch = 0;
+    size_t long_at[kNumTiers] = {};
+    Carve arena;
     const int last = c.max_seq_len > (uint32_t)kLongSmemDistance ? 6 : 5;
     for (int t = 0; t <= last; ++t) {
         const TierShape sh = tier_shape(t, c.max_seq_len, c.cigar_stride, ctx->sm_count);
         if (sh.grid <= 0) continue;
         if (t >= 2 && t <= 4) {
             ctx->scratch_ctas[t] = sh.grid;
-            scratch = std::max(scratch, tier_scratch_bytes(t, sh.grid));
+            scratch = std::max(scratch, tier_scratch_bytes(t, sh.grid, c.max_seq_len));
         } else if (t >= 5) {
             /* a slab per resident CTA (backtrace store, chain, runs; tier 6
              * also its wavefront), the grid trimmed to a budget */
@@ -426,13 +455,54 @@ int create_context(const wfe_config* cfg, uint64_t budget5, uint64_t budget6, wf
             const int grid = (int)std::min<uint64_t>((uint64_t)sh.grid, std::max<uint64_t>(1, budget / sh.slab));
             ctx->scratch_ctas[t] = grid;
             ctx->long_slab[t] = sh.slab;
-            if ((e = cudaMalloc(&ctx->d_long_scratch[t], (size_t)sh.slab * grid)) != cudaSuccess) return bail(e);
+            long_at[t] = arena.take((size_t)sh.slab * grid) + 1u; /* + 1: 0 means none */
         }
     }
+    const size_t ops_at = scratch ? arena.take(scratch) : 0u;
+    const size_t nctr = 2 * kNumTiers + kMaxBuckets;
+    const size_t passed_at = arena.take(sizeof(unsigned long long) * nctr);
+    const size_t B = c.batch_size;
+    size_t lists_at[kStages], counts_at[kStages], pred_at[kStages];
+    for (int i = 0; i < kStages; ++i) {
+        /* a work list per tier of one length bucket; wfe_set_policy adds
+         * room for more buckets */
+        lists_at[i] = arena.take((size_t)kNumTiers * B * sizeof(uint32_t));
+        counts_at[i] = arena.take(sizeof(uint32_t) * kCountWords);
+        pred_at[i] = arena.take(B * sizeof(uint16_t));
+    }
+    /* Host calls of several batches keep two in flight, and the second
+     * stage then needs its own tier scratch: reserve it now, in the same
+     * allocation, rather than in the middle of the first such call.  (A
+     * device-only context allocates it at its first device call of several
+     * batches; see ensure_stage_scratch.) */
+    const bool host_pipeline = !(c.flags & (WFE_FLAG_DEVICE_ONLY | WFE_FLAG_NO_PIPELINE));
+    size_t own_ops_at = 0, own_long_at[kNumTiers] = {};
+    if (host_pipeline) {
+        if (scratch) own_ops_at = arena.take(scratch);
+        for (int t = 5; t < kNumTiers; ++t)
+            if (long_at[t]) own_long_at[t] = arena.take((size_t)ctx->long_slab[t] * ctx->scratch_ctas[t]) + 1u;
+    }
+    if ((e = cudaMalloc(&ctx->d_arena, arena.used)) != cudaSuccess) return bail(e);
+    unsigned char* A0 = ctx->d_arena;
+    for (int t = 5; t < kNumTiers; ++t)
+        if (long_at[t]) ctx->d_long_scratch[t] = A0 + (long_at[t] - 1u);
     if (scratch) {
-        e = cudaMalloc(&ctx->d_ops_scratch, scratch);
-        if (e != cudaSuccess) return bail(e);
+        ctx->d_ops_scratch = A0 + ops_at;
         ctx->ops_scratch_bytes = scratch;
+    }
+    ctx->d_passed = reinterpret_cast<unsigned long long*>(A0 + passed_at);
+    for (int i = 0; i < kStages; ++i) {
+        Stage& s = ctx->st[i];
+        s.d_lists = reinterpret_cast<uint32_t*>(A0 + lists_at[i]);
+        s.d_counts = reinterpret_cast<uint32_t*>(A0 + counts_at[i]);
+        s.d_pred = reinterpret_cast<uint16_t*>(A0 + pred_at[i]);
+    }
+    if (host_pipeline) {
+        Stage& s1 = ctx->st[1];
+        if (scratch) s1.own_ops_scratch = A0 + own_ops_at;
+        for (int t = 5; t < kNumTiers; ++t)
+            if (own_long_at[t]) s1.own_long_scratch[t] = A0 + (own_long_at[t] - 1u);
+        s1.own_scratch = true;
     }
     ctx->nbuckets = 1;
     ctx->bucket[0].max_len = c.max_seq_len;
@@ -440,27 +510,36 @@ int create_context(const wfe_config* cfg, uint64_t budget5, uint64_t budget6, wf
     plan_bucket(ctx, ctx->bucket[0]);
     if (!bucket_usable(ctx->bucket[0])) return bail(cudaErrorInvalidValue); /* sequences too long for shared memory */
 
-    const size_t nctr = 2 * kNumTiers + kMaxBuckets;
-    if ((e = cudaMalloc(&ctx->d_passed, sizeof(unsigned long long) * nctr)) != cudaSuccess) return bail(e);
-    if ((e = cudaMemset(ctx->d_passed, 0, sizeof(unsigned long long) * nctr)) != cudaSuccess) return bail(e);
     ctx->d_launched = ctx->d_passed + kNumTiers;
     ctx->d_bucket_total = ctx->d_passed + 2 * kNumTiers;
-    if ((e = cudaHostAlloc(&ctx->h_launch_error, sizeof(uint32_t), cudaHostAllocMapped)) != cudaSuccess)
-        return bail(e);
-    *ctx->h_launch_error = 0u;
-    if ((e = cudaHostGetDevicePointer(&ctx->d_launch_error, ctx->h_launch_error, 0)) != cudaSuccess) return bail(e);
-    const size_t B = c.batch_size;
+    /* The record of failed device-side launches is host memory the kernels
+     * write in place.  A device that reads the CPU's page tables (ATS over
+     * NVLink-C2C) writes ordinary heap memory; elsewhere it is a mapped
+     * page-locked word (cudaHostAlloc costs ~0.15 ms, and as much to free). */
+    if (ctx->host_page_tables) {
+        uint64_t* w = new (std::nothrow) uint64_t[1];
+        if (!w) return bail(cudaErrorMemoryAllocation);
+        *w = 0u; /* the page is present before the device can write it */
+        ctx->h_launch_error = ctx->d_launch_error = reinterpret_cast<uint8_t*>(w);
+    } else {
+        if ((e = cudaHostAlloc(&ctx->h_launch_error, kLaunchErrorBytes, cudaHostAllocMapped)) != cudaSuccess)
+            return bail(e);
+        ctx->launch_error_pinned = true;
+        std::memset(ctx->h_launch_error, 0, kLaunchErrorBytes);
+        if ((e = cudaHostGetDevicePointer(&ctx->d_launch_error, ctx->h_launch_error, 0)) != cudaSuccess)
+            return bail(e);
+    }
     const bool host_calls = !(c.flags & WFE_FLAG_DEVICE_ONLY);
     for (auto& s : ctx->st) {
         if ((e = cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e);
-        /* a work list per length bucket and tier */
-        if ((e = cudaMalloc(&s.d_lists, kLists * B * sizeof(uint32_t))) != cudaSuccess) return bail(e);
-        if ((e = cudaMalloc(&s.d_counts, sizeof(uint32_t) * kCountWords)) != cudaSuccess) return bail(e);
-        if ((e = cudaMalloc(&s.d_pred, B * sizeof(uint16_t))) != cudaSuccess) return bail(e);
         /* the staging buffers of host calls are allocated by the first call
          * that stages (see ensure_staging) */
         if (host_calls) s.ascii_cap = B * 2u * (size_t)c.max_seq_len + 64u;
     }
+    /* the counters start at zero; both stages' streams come after this */
+    if ((e = cudaMemsetAsync(ctx->d_passed, 0, sizeof(unsigned long long) * nctr, ctx->st[0].stream)) != cudaSuccess)
+        return bail(e);
+    if ((e = cudaStreamSynchronize(ctx->st[0].stream)) != cudaSuccess) return bail(e);
     *out = ctx;
     return WFE_OK;
 }
@@ -500,6 +579,16 @@ int wfe_set_policy(wfe_ctx* ctx, uint32_t nbuckets, const uint32_t* bucket_max_l
     }
     WFE_CUDA(ctx, cudaSetDevice(ctx->cfg.device));
     for (auto& s : ctx->st) WFE_CUDA(ctx, cudaStreamSynchronize(s.stream));
+    if ((int)nbuckets > ctx->lists_buckets) {
+        /* work lists for every tier of every bucket, both stages */
+        const size_t per_stage = (size_t)nbuckets * kNumTiers * ctx->cfg.batch_size;
+        uint32_t* lists = nullptr;
+        WFE_CUDA(ctx, cudaMalloc(&lists, kStages * per_stage * sizeof(uint32_t)));
+        cudaFree(ctx->d_lists_ext);
+        ctx->d_lists_ext = lists;
+        for (int i = 0; i < kStages; ++i) ctx->st[i].d_lists = lists + (size_t)i * per_stage;
+        ctx->lists_buckets = (int)nbuckets;
+    }
     ctx->nbuckets = (int)nbuckets;
     for (uint32_t b = 0; b < nbuckets; ++b) ctx->bucket[b] = plan[b];
     ctx->predict = (flags & WFE_POLICY_PREDICT) != 0;
@@ -523,14 +612,12 @@ void wfe_destroy(wfe_ctx* ctx)
 {
     if (!ctx) return;
     cudaSetDevice(ctx->cfg.device);
-    for (auto& s : ctx->st) {
+    for (auto& s : ctx->st)
         if (s.stream) cudaStreamSynchronize(s.stream);
-        free_stage(s);
-    }
-    cudaFree(ctx->d_ops_scratch);
-    cudaFree(ctx->d_passed);
-    cudaFreeHost(ctx->h_launch_error);
-    for (auto p : ctx->d_long_scratch) cudaFree(p);
+    for (auto& s : ctx->st) free_stage(s);
+    cudaFree(ctx->d_arena);
+    cudaFree(ctx->d_lists_ext);
+    free_launch_error(ctx);
     for (auto& t : ctx->timed) {
         cudaEventDestroy(t.start);
         cudaEventDestroy(t.stop);
@@ -817,23 +904,27 @@ private:
  * need them).  A failed allocation leaves none of them behind. */
 int ensure_staging(wfe_ctx* ctx, Stage& s)
 {
-    if (s.d_ascii) return WFE_OK;
+    if (s.staging_arena) return WFE_OK;
     const size_t B = ctx->cfg.batch_size;
-    cudaError_t e = cudaSuccess;
-    if ((e = cudaMalloc(&s.d_ascii, s.ascii_cap)) == cudaSuccess &&
-        (e = cudaMalloc(&s.d_pairs, B * sizeof(wfe_pair))) == cudaSuccess &&
-        (e = cudaMalloc(&s.d_plen, B * sizeof(uint32_t))) == cudaSuccess &&
-        (e = cudaMalloc(&s.d_tlen, B * sizeof(uint32_t))) == cudaSuccess &&
-        (e = cudaMalloc(&s.d_dist, B * sizeof(int32_t))) == cudaSuccess &&
-        (e = cudaMalloc(&s.d_cigar, B * (size_t)ctx->cfg.cigar_stride + 16u)) == cudaSuccess &&
-        (e = cudaMalloc(&s.d_status, B)) == cudaSuccess)
-        return WFE_OK;
-    for (void** p : {(void**)&s.d_ascii, (void**)&s.d_pairs, (void**)&s.d_plen, (void**)&s.d_tlen,
-                     (void**)&s.d_dist, (void**)&s.d_cigar, (void**)&s.d_status}) {
-        cudaFree(*p);
-        *p = nullptr;
+    Carve c;
+    const size_t ascii_at = c.take(s.ascii_cap), pairs_at = c.take(B * sizeof(wfe_pair));
+    const size_t plen_at = c.take(B * sizeof(uint32_t)), tlen_at = c.take(B * sizeof(uint32_t));
+    const size_t dist_at = c.take(B * sizeof(int32_t));
+    const size_t cigar_at = c.take(B * (size_t)ctx->cfg.cigar_stride + 16u), status_at = c.take(B);
+    const cudaError_t e = cudaMalloc(&s.staging_arena, c.used);
+    if (e != cudaSuccess) {
+        s.staging_arena = nullptr;
+        return fail_cuda(ctx, e);
     }
-    return fail_cuda(ctx, e);
+    unsigned char* a = s.staging_arena;
+    s.d_ascii = reinterpret_cast<char*>(a + ascii_at);
+    s.d_pairs = reinterpret_cast<wfe_pair*>(a + pairs_at);
+    s.d_plen = reinterpret_cast<uint32_t*>(a + plen_at);
+    s.d_tlen = reinterpret_cast<uint32_t*>(a + tlen_at);
+    s.d_dist = reinterpret_cast<int32_t*>(a + dist_at);
+    s.d_cigar = reinterpret_cast<int8_t*>(a + cigar_at);
+    s.d_status = reinterpret_cast<uint8_t*>(a + status_at);
+    return WFE_OK;
 }
 
 /* Stage 1's own scratch of tiers 2-6, the size of the context's, allocated
@@ -842,19 +933,21 @@ int ensure_staging(wfe_ctx* ctx, Stage& s)
 int ensure_stage_scratch(wfe_ctx* ctx, Stage& s)
 {
     if (s.own_scratch) return WFE_OK;
-    cudaError_t e = cudaSuccess;
-    if (ctx->d_ops_scratch) e = cudaMalloc(&s.own_ops_scratch, ctx->ops_scratch_bytes);
-    for (int t = 5; t < kNumTiers && e == cudaSuccess; ++t)
+    Carve c;
+    const size_t ops_at = ctx->d_ops_scratch ? c.take(ctx->ops_scratch_bytes) : 0u;
+    size_t long_at[kNumTiers] = {};
+    for (int t = 5; t < kNumTiers; ++t)
         if (ctx->d_long_scratch[t])
-            e = cudaMalloc(&s.own_long_scratch[t], (size_t)ctx->long_slab[t] * (size_t)ctx->scratch_ctas[t]);
-    if (e != cudaSuccess) {
-        cudaFree(s.own_ops_scratch);
-        s.own_ops_scratch = nullptr;
-        for (auto& p : s.own_long_scratch) {
-            cudaFree(p);
-            p = nullptr;
+            long_at[t] = c.take((size_t)ctx->long_slab[t] * (size_t)ctx->scratch_ctas[t]) + 1u; /* 0: none */
+    if (c.used) {
+        const cudaError_t e = cudaMalloc(&s.scratch_arena, c.used);
+        if (e != cudaSuccess) {
+            s.scratch_arena = nullptr;
+            return fail_cuda(ctx, e);
         }
-        return fail_cuda(ctx, e);
+        if (ctx->d_ops_scratch) s.own_ops_scratch = s.scratch_arena + ops_at;
+        for (int t = 5; t < kNumTiers; ++t)
+            if (long_at[t]) s.own_long_scratch[t] = s.scratch_arena + (long_at[t] - 1u);
     }
     s.own_scratch = true;
     return WFE_OK;

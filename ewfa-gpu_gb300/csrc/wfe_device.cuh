@@ -183,15 +183,22 @@ __device__ __forceinline__ void load_packed(const char* s, uint32_t len, uint2* 
  * lanes read the span in consecutive blocks -- whole 512-byte rows per
  * instruction instead of one short run per group, which the CPU-GPU link
  * serves 20% faster -- pack every block to a 32-bit word and keep the words
- * in `words` (SPAN per warp).  Every byte read lies in a 16-byte block that
- * holds a base of one of the pairs, as with load_packed.  Returns the
- * span's first block address (16-aligned), or 0 when the span is too long
- * (then nothing was read).  All 32 lanes call; p/t/lp/lt are the calling
- * lane's group's pair (lengths 0 for a group without one). */
+ * in `words` (SPAN per warp).  Every aligned block of [lo, hi) is read --
+ * lo the warp's lowest base address, hi one past its highest -- including
+ * blocks that fall in gaps between the pairs and hold none of their bases.
+ * That is safe because the span is at most SPAN * 16 bytes, less than one
+ * 4 KiB page: the whole span lies within the page of its first block and
+ * the page of its last, and both of those blocks hold a base, so both pages
+ * are mapped.  A SPAN above 256 would break that argument (the static
+ * assertion below).  Returns the span's first block address (16-aligned), or
+ * 0 when the span is too long (then nothing was read).  All 32 lanes call;
+ * p/t/lp/lt are the calling lane's group's pair (lengths 0 for a group
+ * without one). */
 template <int SPAN>
 __device__ __forceinline__ uintptr_t load_warp_span(const char* p, uint32_t lp, const char* t, uint32_t lt,
                                                     uint32_t* words, int lane)
 {
+    static_assert(SPAN * 16 <= 4096, "a span must fit in one 4 KiB page (see above)");
     unsigned long long lo = ~0ull, hi = 0ull;
     if (lp) {
         lo = min(lo, (unsigned long long)(uintptr_t)p);

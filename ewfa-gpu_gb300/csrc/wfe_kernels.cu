@@ -120,13 +120,20 @@ struct Tier {
         return !TRI ? 2 * J : (J + (d + G / 2) / G > 2 * J ? 2 * J : J + (d + G / 2) / G);
     }
     static __host__ __device__ constexpr int row_entries(int d) { return chunk_hi(d) - chunk_lo(d) + 1; }
-    static constexpr int store_entries()
+    /* entries of rows 1..rows */
+    static constexpr int store_entries(int rows = DCAP)
     {
         int t = 0;
-        for (int d = 1; d <= DCAP; ++d) t += row_entries(d);
+        for (int d = 1; d <= rows && d <= DCAP; ++d) t += row_entries(d);
         return t;
     }
     static constexpr size_t ops_bytes = round16(sizeof(E) * (size_t)store_entries());
+    /* one group's store for distances up to max_len */
+    static size_t store_bytes(uint32_t max_len)
+    {
+        return round16(sizeof(E) * (size_t)store_entries((int)std::min<uint32_t>(max_len, (uint32_t)DCAP)));
+    }
+    static int store_rows(uint32_t max_len) { return (int)std::min<uint32_t>(max_len, (uint32_t)DCAP); }
     static constexpr size_t chain_bytes = round16((size_t)DCAP + 1);
     static constexpr size_t runs_bytes = round16(sizeof(int) * ((size_t)DCAP + 1));
 };
@@ -195,6 +202,17 @@ using T2 = Tier<32, 4, false, 1>;  /* distance <= 143; backtrace store in global
 using T3 = Tier<32, 8, false, 1>;  /* distance <= 271 */
 using T4 = Tier<32, 16, false, 1>; /* distance <= 527 */
 
+/* Record that the device-side launch of tier u failed: a plain store of one
+ * byte (one per tier, so no two writers share a byte) into host memory that
+ * the host reads once the chain has completed. */
+__device__ __forceinline__ void note_launch_error(const AlignLaunch& A, int u)
+{
+    if (A.chain.launch_error) {
+        *reinterpret_cast<volatile uint8_t*>(A.chain.launch_error + u) = 1u;
+        __threadfence_system();
+    }
+}
+
 /* Tail launch of tier u over its list of `count` pairs, built in the launch's
  * own parameter buffer: A (a __grid_constant__ kernel parameter, read in
  * place) is copied word by word and the per-tier fields are patched.  No
@@ -207,7 +225,7 @@ __device__ __forceinline__ void tail_launch(K kernel, const AlignLaunch& A, int 
 {
     void* buf = cudaGetParameterBufferV2((void*)kernel, dim3((unsigned)grid), dim3((unsigned)threads), smem);
     if (!buf) {
-        if (A.chain.launch_error) atomicOr_system(A.chain.launch_error, 1u << u);
+        note_launch_error(A, u);
         return;
     }
     const unsigned long long* src = reinterpret_cast<const unsigned long long*>(&A);
@@ -228,7 +246,7 @@ __device__ __forceinline__ void tail_launch(K kernel, const AlignLaunch& A, int 
         extra[1] = gbytes;
     }
     if (cudaLaunchDeviceV2(buf, cudaStreamTailLaunch) != cudaSuccess) {
-        if (A.chain.launch_error) atomicOr_system(A.chain.launch_error, 1u << u);
+        note_launch_error(A, u);
         return;
     }
     if (A.chain.launched) atomicAdd(A.chain.launched + u, 1ull);
@@ -309,11 +327,17 @@ __device__ __forceinline__ void tier_body(const AlignLaunch& A, uint32_t seq_wor
     uint8_t* chain = gs + 16u * (size_t)seq_words;
     unsigned char* uni = chain + T::chain_bytes;
     E* ops;
+    /* last score step the backtrace store holds: a pair that would go past
+     * it (never expected: a distance is at most the longest sequence, and
+     * the store holds that many rows) goes on to the next tier instead */
+    int store_last = DCAP;
     if constexpr (T::SMEM_OPS) {
         ops = reinterpret_cast<E*>(uni);
     } else {
+        const TierShape& tsh = A.chain.shape[A.tier];
         const size_t gslot = (size_t)blockIdx.x * (kWarps * GPW) + (size_t)slot;
-        ops = reinterpret_cast<E*>(A.ops_scratch + gslot * T::ops_bytes);
+        ops = reinterpret_cast<E*>(A.ops_scratch + gslot * tsh.ops_group_bytes);
+        store_last = min(DCAP, tsh.ops_rows);
     }
     int8_t* stage = reinterpret_cast<int8_t*>(uni);
     int* runs = reinterpret_cast<int*>(uni + round16(A.cigar_stride));
@@ -380,7 +404,7 @@ __device__ __forceinline__ void tier_body(const AlignLaunch& A, uint32_t seq_wor
         for (int d = 1;; rowbase += T::row_entries(d), ++d) {
             const bool run = state == ST_RUN;
             if (!__any_sync(kFull, run)) break;
-            if (d > DCAP || (A.max_distance > 0 && d > A.max_distance)) {
+            if (d > store_last || (A.max_distance > 0 && d > A.max_distance)) {
                 if (run) state = (A.max_distance > 0 && d > A.max_distance) ? ST_OVERMAX : ST_OVERFLOW;
                 break;
             }
@@ -731,6 +755,10 @@ TierShape shape_of(uint32_t max_len, uint32_t cigar_stride, int sm_count)
     sh.smem = (uint32_t)smem;
     sh.seq_words = seq_words_for(max_len);
     sh.gbytes = (uint32_t)group_smem_bytes<T>(max_len, cigar_stride);
+    if (!T::SMEM_OPS) {
+        sh.ops_group_bytes = (uint32_t)T::store_bytes(max_len);
+        sh.ops_rows = T::store_rows(max_len);
+    }
     return sh;
 }
 
@@ -747,8 +775,12 @@ cudaError_t launch(const AlignLaunch& a, int grid, cudaStream_t s)
     const size_t gb = group_smem_bytes<T>(a.max_len, a.cigar_stride);
     const size_t smem = cta_smem_bytes<T>(a.max_len, a.cigar_stride);
     if (smem > 227u * 1024u) return cudaErrorInvalidValue;
-    if (!T::SMEM_OPS && a.ops_scratch_bytes < T::ops_bytes * (size_t)grid * (kWarps * T::GPW))
-        return cudaErrorInvalidValue;
+    if (!T::SMEM_OPS) {
+        const TierShape& tsh = a.chain.shape[a.tier];
+        if (tsh.ops_group_bytes == 0 || tsh.ops_rows <= 0 ||
+            a.ops_scratch_bytes < (size_t)tsh.ops_group_bytes * (size_t)grid * (kWarps * T::GPW))
+            return cudaErrorInvalidValue;
+    }
     cudaError_t e = allow_smem(host_kernel<T>(), smem);
     if (e != cudaSuccess) return e;
     if constexpr (T::G == 32)
@@ -938,12 +970,12 @@ history_cigar_kernel(Layout L, uint32_t n, uint32_t max_len, const int32_t* dist
 
 const TierInfo& tier_info(int t) { return kTiers[t]; }
 
-size_t tier_scratch_bytes(int tier, int grid)
+size_t tier_scratch_bytes(int tier, int grid, uint32_t max_len)
 {
     switch (tier) {
-    case 2: return T2::ops_bytes * (size_t)grid * (kWarps * T2::GPW);
-    case 3: return T3::ops_bytes * (size_t)grid * (kWarps * T3::GPW);
-    case 4: return T4::ops_bytes * (size_t)grid * (kWarps * T4::GPW);
+    case 2: return T2::store_bytes(max_len) * (size_t)grid * (kWarps * T2::GPW);
+    case 3: return T3::store_bytes(max_len) * (size_t)grid * (kWarps * T3::GPW);
+    case 4: return T4::store_bytes(max_len) * (size_t)grid * (kWarps * T4::GPW);
     default: return 0;
     }
 }

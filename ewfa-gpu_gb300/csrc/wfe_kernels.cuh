@@ -35,6 +35,9 @@ struct TierShape {
     int dlim;           /* tiers 5-6: largest distance the tier computes */
     uint64_t slab;      /* tiers 5-6: bytes of global scratch per CTA */
     unsigned char* scratch; /* tiers 5-6: grid * slab bytes */
+    uint32_t ops_group_bytes; /* tiers 2-4: bytes of one group's backtrace store in the global scratch */
+    int ops_rows;       /* tiers 2-4: score steps that store holds (a distance never exceeds the
+                           longest sequence, so rows past max_len are never written) */
 };
 
 /* Global scratch of one CTA of tiers 5-6 for distances up to dlim: 2-bit
@@ -56,7 +59,8 @@ struct Chain {
     uint32_t* work_next;             /* work_next[t]: next work item of tier t (work stealing) */
     unsigned long long* launched;    /* launched[t]: launches of tier t (stats) */
     unsigned long long* passed;      /* passed[t]: pairs tier t handed on (stats) */
-    uint32_t* launch_error;          /* bit t: a device-side launch of tier t failed (host-mapped) */
+    uint8_t* launch_error;           /* byte t set: a device-side launch of tier t failed (host memory
+                                        the device writes in place) */
 };
 
 /* Length buckets of the classify kernel, and for each the tiers a pair may
@@ -104,8 +108,10 @@ struct AlignLaunch {
  * cigar_stride: persistent grid sized by occupancy (grid 0: does not fit). */
 TierShape tier_shape(int tier, uint32_t max_len, uint32_t cigar_stride, int sm_count);
 
-/* Bytes of global op-store scratch tier t needs for `grid` CTAs. */
-size_t tier_scratch_bytes(int tier, int grid);
+/* Bytes of global op-store scratch tier t needs for `grid` CTAs, each
+ * group's store holding the rows of distances up to max_len (capped at the
+ * tier's own limit). */
+size_t tier_scratch_bytes(int tier, int grid, uint32_t max_len);
 /* Persistent grid of tier t for sequences up to max_len, cigar slots of
  * cigar_stride (occupancy-limited, at least 1). */
 int tier_grid(int tier, uint32_t max_len, uint32_t cigar_stride, int sm_count);

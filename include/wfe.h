@@ -320,13 +320,19 @@ int wfe_cigar_from_history_device(const char* d_ascii, const wfe_pair* d_pairs,
  * cigar_stride do not fit the kernel's shared memory.
  *
  * Scratch: a WFE_NOALLOC_SCRATCH_BYTES array in the library's device image,
- * held by every GPU that loads the library until the process exits.  The
- * first call on a device looks up that array's device address (set-up, once
- * per device); make that first call outside any stream capture.  Every call
- * shares the array and it keeps the last call's contents (nothing in it has
- * to start at zero: each entry is written before it is read).  Calls that
- * overlap on the GPU -- on two streams, or from two host threads -- race on
- * the array and corrupt each other's results: issue them on one stream. */
+ * held by every GPU that loads the library until the process exits.  Its
+ * device address belongs to the CUDA context current at call time (the
+ * device's primary context, or one the application made current); the first
+ * call in each context looks that address up (set-up, once per context),
+ * so make that first call outside any stream capture.  The array holds the
+ * backtrace stores of 816 pairs in flight, so a call runs at most 204 CTAs
+ * of 4 pairs: about 1.3 per SM on a 152-SM GB300, below the kernel's
+ * occupancy, so a call is slower than wfe_align_device on the same pairs.
+ * Every call shares the array and it
+ * keeps the last call's contents (nothing in it has to start at zero: each
+ * entry is written before it is read).  Calls that overlap on the GPU -- on
+ * two streams, or from two host threads -- race on the array and corrupt
+ * each other's results: issue them on one stream. */
 int wfe_align_device_noalloc(const char* d_ascii, const wfe_pair* d_pairs, size_t n,
                              uint32_t max_len, int32_t max_distance, int32_t* d_dist,
                              int8_t* d_cigar, uint32_t cigar_stride, uint8_t* d_status,

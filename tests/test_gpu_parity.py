@@ -711,12 +711,15 @@ def test_exhaustive_tiny_pairs():
 
 def test_allocation_failure_is_reported_and_leaves_the_device_usable():
     """Buffers that cannot be allocated give WFE_ERR_OUT_OF_MEMORY: at
-    creation (the work lists) or at the first call that stages (the staging
-    buffers); nothing is left half-made, in-place calls on such a context
-    still work, and the next context works."""
+    creation (the context's device buffers) or at the first call that stages
+    (the staging buffers); nothing is left half-made, in-place calls on such a
+    context still work, and the next context works."""
     torch_cuda()
     with pytest.raises(wfe.WfeError) as e:
-        wfe.Context(max_seq_len=300, batch_size=4_000_000_000)  # 896 GB of work lists per stage
+        # sequences of 50,000 bases: a slab of the global-wavefront tier holds a
+        # backtrace store of ~625 MB, and a 1 TB slab budget asks for one per
+        # resident CTA, several hundred GB
+        wfe.Context(max_seq_len=50_000, batch_size=1000, cigar_stride=4096, long_scratch=(0, 1 << 40))
     assert e.value.code == wfe.ERR_OUT_OF_MEMORY
     ascii, pairs = wfe.generate(2000, 150, p_min=0.05, seed=9)
     # 200M pairs per batch: 45 GB of work lists per stage fit, 120 GB of ASCII staging does not

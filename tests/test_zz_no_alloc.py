@@ -79,3 +79,70 @@ def test_noalloc_rejects_search_ranges_beyond_its_scratch():
         with pytest.raises(wfe.WfeError) as e:
             wfe.align_device_noalloc(d_ascii, d_pairs, 8, 300, bad, out, cg, 152, None)
         assert e.value.code == wfe.ERR_INVALID_ARGUMENT
+
+
+def test_noalloc_matches_the_oracle_and_allocates_nothing():
+    """Direct parity with the CPU restatement of the reference, one pair over
+    max_len (WFE_PAIR_TOO_LONG, as wfe_align_device reports it), and no
+    change in the device's free memory across a call."""
+    import torch
+
+    import oracle
+
+    stride, max_len, cap = 152, 150, 63
+    a, p = wfe.generate(6000, 140, 160, p_min=0.02, p_max=0.12, seed=33)
+    n = len(p)
+    d_ascii = torch.from_numpy(a).cuda()
+    d_pairs = torch.from_numpy(p.view(np.uint8)).cuda()
+    dist = torch.full((n,), -7, dtype=torch.int32, device="cuda")
+    cg = torch.full((n * stride,), 55, dtype=torch.int8, device="cuda")
+    st = torch.full((n,), 99, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.Stream()
+    wfe.align_device_noalloc(d_ascii, d_pairs, n, max_len, cap, dist, cg, stride, st, stream)  # set-up call
+    stream.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    wfe.align_device_noalloc(d_ascii, d_pairs, n, max_len, cap, dist, cg, stride, st, stream)
+    stream.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, f"free device memory changed by {free0 - free1} bytes across a call"
+
+    too_long = np.maximum(p["p_len"], p["t_len"]) > max_len
+    assert too_long.any() and (~too_long).any()
+    b_d, b_s = dist.cpu().numpy(), st.cpu().numpy()
+    b_c = cg.cpu().numpy().reshape(n, stride)
+    assert (b_s[too_long] == wfe.PAIR_TOO_LONG).all()
+    assert (b_d[too_long] == -1).all()
+    od, ocg, ost, _ = oracle.align_batch(a, p["p_off"], p["p_len"], p["t_off"], p["t_len"], stride, max_distance=cap)
+    ok = ~too_long
+    np.testing.assert_array_equal(b_d[ok], od[ok])
+    np.testing.assert_array_equal(b_s[ok], ost[ok])
+    assert (ost[ok] == wfe.PAIR_OVER_MAX_DISTANCE).any() or b_d[ok].max() > 10
+    for i in np.flatnonzero(ok & (ost == wfe.PAIR_OK)):
+        assert _cigar_bytes(b_c[i]) == _cigar_bytes(ocg[i]), f"pair {i}"
+
+    # the same pairs through wfe_align_device agree on the too-long ones too
+    ref_d = torch.zeros(n, dtype=torch.int32, device="cuda")
+    ref_c = torch.zeros(n * stride, dtype=torch.int8, device="cuda")
+    ref_s = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    with wfe.Context(max_seq_len=max_len, max_distance=cap, cigar_stride=stride) as ctx:
+        ctx.align_device(d_ascii, d_pairs, n, max_len, ref_d, ref_c, ref_s, stream)
+        stream.synchronize()
+    np.testing.assert_array_equal(b_d, ref_d.cpu().numpy())
+    np.testing.assert_array_equal(b_s, ref_s.cpu().numpy())
+
+
+def test_noalloc_without_status_or_cigars():
+    """d_status NULL and cigar_stride 0: distances only, still the oracle's."""
+    import torch
+
+    import oracle
+
+    a, p = wfe.generate(3000, 150, p_min=0.05, seed=34)
+    n = len(p)
+    d_ascii = torch.from_numpy(a).cuda()
+    d_pairs = torch.from_numpy(p.view(np.uint8)).cuda()
+    dist = torch.full((n,), -7, dtype=torch.int32, device="cuda")
+    wfe.align_device_noalloc(d_ascii, d_pairs, n, 300, 63, dist, None, 0, None, None)
+    torch.cuda.synchronize()
+    od, _, _, _ = oracle.align_batch(a, p["p_off"], p["p_len"], p["t_off"], p["t_len"], 152, max_distance=63)
+    np.testing.assert_array_equal(dist.cpu().numpy(), od)
