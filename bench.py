@@ -72,12 +72,16 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-other-workloads", action="store_true",
+                    help="short workload: skip the long, mixed and serve runs that the line reports beside it")
     ap.add_argument("--workload", choices=["short", "long", "mixed", "serve"], default="short",
                     help="short: the short-read throughput workload (the metric's configuration); "
                          "long: 200,000 pairs of 1,000 bases at edit probability 0.10; "
                          "mixed: uneven lengths, plain fixed-shape launches vs length buckets; "
                          "serve: Poisson request stream, the request server vs one call per request")
     ap.add_argument("--requests", type=int, default=0, help="serve workload: number of requests (default 1,000)")
+    ap.add_argument("--rates", default="", help="serve workload: loads as fractions of the measured peak, "
+                                                 "comma-separated (default 0.1,0.25,0.5,0.75,0.9,1.0,1.2)")
     ap.add_argument("--pairs", type=int, default=0, help="mixed workload: number of pairs (default 2,000,000)")
     ap.add_argument("--profile-batch", type=int, default=0,
                     help="profiling case: run the --profile-kernel kernels twice over ONE batch of this "
@@ -304,8 +308,146 @@ def run_mixed(args) -> int:
                       res[m]["seconds"] / 1e9 for m in modes},
             "identical_results": same_dist and same_status, "all_ok": ok_status,
             "distance": {"mean": float(dist.mean()), "max": int(dist.max())}}
+    b_dist, b_st, b_cg = outs["bucketed"]
+    line["parity"] = oracle_sample_parity(ascii, pairs, (b_dist, b_cg, b_st), stride, MIXED_SEED)
+    del outs
+    line["ref_cuda"] = reference_on_subset(ascii, pairs, b_dist, b_st, b_cg, MIXED_BUCKETS, stride, MIXED_SEED)
     print(json.dumps(line))
-    return 0 if same_dist and same_status and ok_status else 1
+    good = same_dist and same_status and ok_status and line["parity"]["mismatches"] == 0
+    return 0 if good else 1
+
+
+ORACLE_SAMPLE = 20_000      # pairs of the mixed and served workloads checked against the CPU oracle
+REF_SUBSET = 100_000        # pairs of the reference's search range aligned by its own kernels
+REF_CLASSES = [256, 512, 1024, 2048, 4096, 11_000]  # length classes, one reference run each
+
+
+def oracle_sample_parity(ascii, pairs, got, stride: int, seed: int) -> dict:
+    """Distances, statuses and CIGARs of a seeded sample of ORACLE_SAMPLE
+    pairs against the CPU restatement of the reference (oracle/).  got =
+    (dist, cigar slots -- numpy or a device tensor of n * stride bytes --,
+    status)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build(ref=False)
+    dist, cg, st = got
+    n = len(pairs)
+    idx = np.sort(np.random.default_rng(seed).choice(n, min(ORACLE_SAMPLE, n), replace=False))
+    if hasattr(cg, "view") and not isinstance(cg, np.ndarray):
+        import torch
+        rows = cg.view(n, stride).index_select(0, torch.from_numpy(idx).to(cg.device)).cpu().numpy()
+    else:
+        rows = np.asarray(cg).reshape(n, stride)[idx]
+    sub = pairs[idx]
+    od, ocg, ost, _ = oracle.align_batch(ascii, sub["p_off"], sub["p_len"], sub["t_off"], sub["t_len"], stride,
+                                         nthreads=os.cpu_count() or 1)
+    rec = parity((np.asarray(dist)[idx], rows, np.asarray(st)[idx]), (od, ocg, ost))
+    rec["sample"] = f"{len(idx):,} seeded pairs of {n:,}"
+    return rec
+
+
+def reference_on_subset(ascii, pairs, dist, status, cg, buckets, stride: int, seed: int) -> dict | None:
+    """The reference's own CUDA kernels (sm_100 cubin) on the pairs of a
+    workload that lie in its search range, distance <= 63
+    (src/wavefront.cuh:462-466): a seeded sample of REF_SUBSET of them, run
+    in length classes (one -l per class, slots of the class's longest
+    sequence: the reference has one slot size per run), its batch loop timed
+    with allocations outside the clock (steady), best of 3; the classes'
+    times add up.  This build aligns the same pairs through wfe_align with
+    pinned host buffers (length buckets and first tiers by the autotuner),
+    best of 3.  The reference's CIGARs are compared with this build's."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    import torch
+    try:
+        oracle.build(ref=False)
+    except Exception:
+        return None
+    if not oracle.ref_cuda_available():
+        return None
+    n = len(pairs)
+    inside = np.flatnonzero((np.asarray(status) == 0) & (np.asarray(dist) <= 63))
+    idx = np.sort(np.random.default_rng(seed + 1).choice(inside, min(REF_SUBSET, len(inside)), replace=False))
+    sub = pairs[idx]
+    # this build's CIGARs of the sample
+    if hasattr(cg, "view") and not isinstance(cg, np.ndarray):
+        ours = cg.view(n, stride).index_select(0, torch.from_numpy(idx).to(cg.device)).cpu().numpy()
+    else:
+        ours = np.asarray(cg).reshape(n, stride)[idx]
+    longest = np.maximum(sub["p_len"], sub["t_len"]).astype(np.int64)
+    ref_s, mismatches, classes = 0.0, 0, []
+    with tempfile.TemporaryDirectory() as tmp:
+        lo = 0
+        for hi in REF_CLASSES:
+            sel = np.flatnonzero((longest > lo) & (longest <= hi))
+            lo = hi
+            if len(sel) == 0:
+                continue
+            slot = (int(longest[sel].max()) + 1) // 2  # the reader's -l: slots of 2 * l bases
+            dump = os.path.join(tmp, f"cigars_{hi}.bin")
+            rec = oracle.ref_cuda_run_pairs(ascii, sub[sel], slot, batch=BATCH, threads=1, reps=3, steady=True,
+                                            dump=dump)
+            ref_s += rec["best_wall_s"]
+            cml = slot + (4 - slot % 4)
+            rc = np.fromfile(dump, np.int8).reshape(len(sel), cml)
+            w = min(cml, stride)
+            mine = ours[sel, :w]
+            lr, lm = cigar_lengths(rc[:, :w]), cigar_lengths(mine)
+            upto = np.arange(w)[None, :] <= lr[:, None]
+            same = (lr == lm) & np.all(np.where(upto, rc[:, :w], 0) == np.where(upto, mine, 0), axis=1)
+            mismatches += int((~same).sum())
+            classes.append({"max_len": hi, "pairs": int(len(sel)), "l": slot, "ref_s": rec["best_wall_s"]})
+    # this build on the same pairs: a compact copy of their sequences in pinned memory
+    h_ascii, h_pairs = compact_pairs(ascii, sub)
+    hp_ascii = torch.empty(len(h_ascii), dtype=torch.uint8, pin_memory=True).numpy()
+    hp_ascii[:] = h_ascii
+    hp_pairs = torch.empty(len(sub) * wfe.PAIR_DTYPE.itemsize, dtype=torch.uint8,
+                           pin_memory=True).numpy().view(wfe.PAIR_DTYPE)
+    hp_pairs[:] = h_pairs
+    m = len(sub)
+    outs = (torch.empty(m, dtype=torch.int32, pin_memory=True).numpy(),
+            torch.empty(m * stride, dtype=torch.int8, pin_memory=True).numpy().reshape(m, stride),
+            torch.empty(m, dtype=torch.uint8, pin_memory=True).numpy())
+    max_seq = int(longest.max())
+    bk = [b for b in buckets if b < max_seq] + [max_seq]
+    cache = os.path.join(tempfile.gettempdir(), "wfe_autotune.jsonl")
+    with wfe.Context(max_seq_len=max_seq, batch_size=BATCH, cigar_stride=stride) as ctx:
+        d_a = torch.from_numpy(h_ascii).cuda()
+        d_p = torch.from_numpy(h_pairs.view(np.uint8)).cuda()
+        tiers = ctx.autotune(d_a, d_p, m, bk, cache)
+        del d_a, d_p
+        ctx.align(hp_ascii, hp_pairs, out=outs)  # warm-up
+        best = 1e30
+        for _ in range(3):
+            t0 = time.perf_counter()
+            ctx.align(hp_ascii, hp_pairs, out=outs)
+            best = min(best, time.perf_counter() - t0)
+    same_as_device = bool(np.array_equal(outs[0], np.asarray(dist)[idx]))
+    return {"subset": "pairs at distance <= 63 (the reference's search range), a seeded sample",
+            "pairs": int(m), "of_pairs_in_range": int(len(inside)), "of_pairs": int(n),
+            "ref_steady": {"value": m / ref_s, "seconds": ref_s, "classes": classes,
+                           "region": "batch loop per class, allocations outside the clock, best of 3"},
+            "e2e": {"value": m / best, "seconds": best, "first_tiers": tiers,
+                    "transfer": "wfe_align, pinned host buffers read and written in place"},
+            "e2e_over_ref_steady": (m / best) / (m / ref_s),
+            "cigars_identical_to_reference": mismatches == 0, "cigar_mismatches": mismatches,
+            "same_as_device_run": same_as_device}
+
+
+def compact_pairs(ascii: np.ndarray, sub: np.ndarray):
+    """The sequences of `sub` copied one after another (pattern, text) into
+    a new buffer, with descriptors into it."""
+    lens = np.stack([sub["p_len"], sub["t_len"]], axis=1).reshape(-1).astype(np.int64)
+    offs = np.stack([sub["p_off"], sub["t_off"]], axis=1).reshape(-1).astype(np.int64)
+    starts = np.concatenate([[0], np.cumsum(lens)[:-1]])
+    total = int(lens.sum())
+    out = np.zeros(total + 64, np.uint8)
+    for o, st, ln in zip(offs.tolist(), starts.tolist(), lens.tolist()):
+        out[st:st + ln] = ascii[o:o + ln]
+    desc = np.zeros(len(sub), wfe.PAIR_DTYPE)
+    desc["p_off"], desc["t_off"] = starts[0::2], starts[1::2]
+    desc["p_len"], desc["t_len"] = sub["p_len"], sub["t_len"]
+    return out, desc
 
 
 SERVE_REQUESTS, SERVE_MAX_PAIRS, SERVE_LMIN, SERVE_LMAX, SERVE_PMIN, SERVE_PMAX, SERVE_SEED = \
@@ -404,7 +546,8 @@ def run_serve(args) -> int:
 
     rows = []
     identical = True
-    for f in SERVE_RATES:
+    rates = [float(x) for x in args.rates.split(",")] if args.rates else SERVE_RATES
+    for f in rates:
         rate = f * peak / float(sizes.mean())  # requests per second
         gaps = rng.exponential(1.0 / rate, nreq)
         row = {"load": f, "offered_alignments_per_s": f * peak}
@@ -439,8 +582,74 @@ def run_serve(args) -> int:
             "rates": rows, "server": st,
             "identical_results": identical and same_cg,
             "all_ok": bool((outs["served"][2] == 0).all())}
+    s_dist, s_cg, s_st = outs["served"]
+    line["parity"] = oracle_sample_parity(ascii, pairs, (s_dist, s_cg, s_st), stride, SERVE_SEED)
+    del outs
+    line["ref_cuda"] = reference_on_subset(ascii, pairs, s_dist, s_st, s_cg, buckets, stride, SERVE_SEED)
     print(json.dumps(line))
-    return 0 if line["identical_results"] and line["all_ok"] else 1
+    good = line["identical_results"] and line["all_ok"] and line["parity"]["mismatches"] == 0
+    return 0 if good else 1
+
+
+def run_other_workloads() -> dict:
+    """The long, mixed and serve workloads, each run by this script in a
+    process of its own (its own CUDA context and memory), summarised for the
+    short-read line: throughput, the checks each makes (identical results
+    between forms, oracle parity) and the reference's kernels on the pairs
+    in its search range."""
+    runs = {"long": ["--steps", "10", "--warmup", "3"], "mixed": [], "serve": ["--rates", "0.5,1.0,1.2"]}
+    out = {}
+    for name, extra in runs.items():
+        cmd = [sys.executable, os.path.abspath(__file__), "--workload", name] + extra
+        t0 = time.perf_counter()
+        try:
+            r = subprocess.run(cmd, capture_output=True, text=True, timeout=900)
+        except subprocess.TimeoutExpired:
+            out[name] = {"error": "timed out after 900 s"}
+            continue
+        lines = [x for x in r.stdout.splitlines() if x.startswith("{")]
+        if r.returncode != 0 or not lines:
+            out[name] = {"error": f"exit {r.returncode}", "stderr": r.stderr[-400:], "stdout": r.stdout[-400:]}
+            continue
+        full = json.loads(lines[-1])
+        out[name] = summarise(name, full)
+        out[name]["run_seconds"] = round(time.perf_counter() - t0, 1)
+        out[name]["command"] = "python bench.py " + " ".join(["--workload", name] + extra)
+    return out
+
+
+def summarise(name: str, d: dict) -> dict:
+    """The fields of a workload's JSON line that the short-read line carries."""
+    if name == "long":
+        return {"workload": d["config"]["workload"], "value": d["value"], "unit": d["unit"],
+                "ms_per_step": d["ms_per_step"], "e2e": d["e2e"]["value"], "gcups": d["gcups"]["value"],
+                "parity": d.get("parity"), "cpu_baseline": (d.get("cpu_baseline") or {}).get("value"),
+                "roofline_frac": d["roofline"]["frac"]}
+    if name == "mixed":
+        keep = ("alignments_per_s", "seconds", "first_tiers")
+        return {"pairs": d["pairs"], "config": d["config"],
+                **{m: {k: d[m][k] for k in keep} for m in ("plain", "bucketed", "predicted")},
+                "speedup_over_plain": d["speedup"], "identical_results": d["identical_results"],
+                "all_ok": d["all_ok"], "parity": d["parity"], "ref_cuda": d.get("ref_cuda"),
+                "distance": d["distance"]}
+    if name == "serve":
+        rows = [{"load": r["load"], "served": {k: r["served"][k] for k in ("p50_ms", "p99_ms", "alignments_per_s")},
+                 "plain": {k: r["plain"][k] for k in ("p50_ms", "p99_ms", "alignments_per_s")}}
+                for r in d["rates"]]
+        return {"config": d["config"], "peak_alignments_per_s": d["peak_alignments_per_s"], "rates": rows,
+                "identical_results": d["identical_results"], "all_ok": d["all_ok"], "parity": d["parity"],
+                "ref_cuda": d.get("ref_cuda")}
+    return d
+
+
+def workload_config(world: int, ascii_bytes: int) -> dict:
+    """The `config` of both arms' JSON lines (identical keys and values)."""
+    nb = PAIRS // BATCH
+    return {"workload": WORKLOAD, "pairs_per_gpu": PAIRS, "batch": BATCH, "length": LENGTH,
+            "edit_prob": EDIT_P, "seed": SEED, "cigar_stride": CIGAR_STRIDE,
+            "l2": (f"inputs larger than L2: steps cycle over {nb} batches "
+                   f"({ascii_bytes / 1e6:.0f} MB ASCII, {PAIRS * CIGAR_STRIDE / 1e6:.0f} MB CIGAR slots)"),
+            "parallelism": f"replicas x{world}"}
 
 
 def dist_env():
@@ -615,17 +824,35 @@ def cigar_lengths(cg: np.ndarray) -> np.ndarray:
 
 def cpu_baseline(ascii, pairs, nthreads):
     """The CPU restatement of the reference (oracle/) on all host cores, on
-    the whole workload (about 1-2 s of CPU time per 1M pairs and core)."""
+    the whole workload (about 1-2 s of CPU time per 1M pairs and core).
+    Returns the baseline record and the oracle's outputs (distances, CIGAR
+    slots, statuses), which the timed runs are then checked against."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build(ref=False)
     t0 = time.perf_counter()
-    _, _, _, (cells, words) = oracle.align_batch(ascii, pairs["p_off"], pairs["p_len"], pairs["t_off"],
-                                                 pairs["t_len"], CIGAR_STRIDE, nthreads=nthreads)
+    dist, cg, st, (cells, words) = oracle.align_batch(ascii, pairs["p_off"], pairs["p_len"], pairs["t_off"],
+                                                      pairs["t_len"], CIGAR_STRIDE, nthreads=nthreads)
     dt = time.perf_counter() - t0
-    return {"value": len(pairs) / dt, "unit": METRIC, "cores": nthreads, "kind": "port",
-            "sample": f"all {len(pairs):,} pairs of the workload, {nthreads} threads, {dt:.2f} s",
-            "counts": {"cells": int(cells), "extend_words": int(words), "pairs": len(pairs)}}
+    return ({"value": len(pairs) / dt, "unit": METRIC, "cores": nthreads, "kind": "port",
+             "sample": f"all {len(pairs):,} pairs of the workload, {nthreads} threads, {dt:.2f} s",
+             "counts": {"cells": int(cells), "extend_words": int(words), "pairs": len(pairs)}},
+            (dist, cg, st))
+
+
+def parity(got, want) -> dict:
+    """Pairs whose distance, status or CIGAR bytes (up to and including the
+    terminator) differ between two result sets (dist, cigar slots, status)."""
+    gd, gc, gs = got
+    wd, wc, ws = want
+    gc = np.asarray(gc).reshape(len(gd), -1)
+    wc = np.asarray(wc).reshape(len(wd), -1)
+    gl, wl = cigar_lengths(gc), cigar_lengths(wc)
+    upto = np.arange(gc.shape[1])[None, :] <= gl[:, None]
+    same_cg = (gl == wl) & np.all(np.where(upto, gc, 0) == np.where(upto, wc, 0), axis=1)
+    bad = (np.asarray(gd) != np.asarray(wd)) | (np.asarray(gs) != np.asarray(ws)) | ~same_cg
+    return {"pairs": int(len(gd)), "mismatches": int(bad.sum()),
+            "compared": "distance, status and the CIGAR bytes up to the terminator of every pair"}
 
 
 def int32_peak(device: int) -> dict | None:
@@ -670,10 +897,15 @@ def int_roofline(base, peak, step_ms, pairs_per_step) -> dict | None:
 def reference_cuda_baseline():
     """The reference's own CUDA kernels (src/kernels.cu compiled for sm_100,
     as its `make SM=100 COMPUTE=100 all` does) through a restatement of its
-    batch loop, timed like its wfe.aligner (wall time from before allocation
-    to after the last batch), on the same workload: -n 1000000 -l 150
-    -b 100000, -t 1/2/4/8, best of 3 each.  None where the kernels were not
-    compiled (they need the reference sources)."""
+    batch loop, on the same workload: -n 1000000 -l 150 -b 100000.
+      value   timed like its wfe.aligner: wall time from before the
+              allocations to after the last batch and the frees
+              (src/aligner.cu:198-233), -t 1/2/4/8, best of 3 each;
+      steady  the batch loop alone: allocations before the clock, frees
+              after it (-t 1/2, best of 3), the region that the e2e figure
+              of wfe_align on an existing context times.
+    None where the kernels were not compiled (they need the reference
+    sources)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     try:
@@ -682,15 +914,108 @@ def reference_cuda_baseline():
         return None
     if not oracle.ref_cuda_available() or LENGTH != 150:
         return None  # the reference searches distances up to 63: only the short-read workload fits
-    runs = {}
+    runs, steady = {}, {}
     for t in (1, 2, 4, 8):
         rec = oracle.ref_cuda_run(PAIRS, LENGTH, EDIT_P, SEED, batch=BATCH, threads=t, reps=3)
         runs[t] = rec["alignments_per_s"]
+    for t in (1, 2):
+        rec = oracle.ref_cuda_run(PAIRS, LENGTH, EDIT_P, SEED, batch=BATCH, threads=t, reps=3, steady=True)
+        steady[t] = rec["alignments_per_s"]
     best_t = max(runs, key=runs.get)
+    best_s = max(steady, key=steady.get)
     return {"value": runs[best_t], "unit": "alignments/s", "threads": best_t,
+            "wall_ms": 1e3 * PAIRS / runs[best_t],
             "by_threads": {str(t): round(v) for t, v in runs.items()},
+            "steady": {"value": steady[best_s], "threads": best_s, "ms": 1e3 * PAIRS / steady[best_s],
+                       "by_threads": {str(t): round(v) for t, v in steady.items()},
+                       "region": "batch loop only: allocations and module load before the clock, frees after"},
             "kind": "reference src/kernels.cu (sm_100 cubin) + restated src/wavefront.cu batch loop, "
                     "wall time as src/aligner.cu:198-233, best of 3"}
+
+
+def cli_wall(reps: int = 5) -> dict | None:
+    """wfe.aligner -f F -n PAIRS -l LENGTH -b BATCH -t 1 on a pair file of
+    the workload (written by wfe.gen with the same generator and seed): the
+    wall time it prints, which covers the reference's region -- after the
+    file is read, context creation and teardown included.  Best and median
+    of `reps` runs."""
+    exe = os.path.join(ROOT, "ewfa-gpu_gb300", "bin", "wfe.aligner")
+    gen = os.path.join(ROOT, "ewfa-gpu_gb300", "bin", "wfe.gen")
+    if not (os.path.exists(exe) and os.path.exists(gen)):
+        return None
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "pairs.seq")
+        subprocess.run([gen, path, str(PAIRS), str(LENGTH), str(LENGTH), str(EDIT_P), str(EDIT_P), str(SEED)],
+                       check=True, stdout=subprocess.DEVNULL)
+        walls = []
+        for _ in range(reps):
+            out = subprocess.run([exe, "-f", path, "-n", str(PAIRS), "-l", str(LENGTH), "-b", str(BATCH), "-t", "1"],
+                                 check=True, capture_output=True, text=True).stdout
+            line = [x for x in out.splitlines() if x.startswith("Aligned executed. Wall time")][-1]
+            walls.append(float(line.split()[-1].rstrip("s")))
+    best = min(walls)
+    return {"value": PAIRS / best, "unit": "alignments/s", "wall_ms": 1e3 * best,
+            "median_wall_ms": 1e3 * statistics.median(walls), "runs": reps,
+            "command": f"wfe.aligner -f pairs.seq -n {PAIRS} -l {LENGTH} -b {BATCH} -t 1",
+            "region": "the reference's: after the file is read; context creation and teardown included"}
+
+
+def noalloc_throughput(d_ascii, d_pairs, want, stream, steps: int) -> dict:
+    """wfe_align_device_noalloc on the device-resident workload: one call per
+    batch (its fixed scratch array bounds the pairs in flight), timed like
+    `value`, results compared with the context path's."""
+    import torch
+    d_dist = torch.zeros(PAIRS, dtype=torch.int32, device=d_ascii.device)
+    d_cigar = torch.zeros(PAIRS * CIGAR_STRIDE, dtype=torch.int8, device=d_ascii.device)
+    d_status = torch.zeros(PAIRS, dtype=torch.uint8, device=d_ascii.device)
+    nb = PAIRS // BATCH
+    pb = wfe.PAIR_DTYPE.itemsize
+
+    def step(i):
+        b = i % nb
+        wfe.align_device_noalloc(d_ascii, d_pairs.data_ptr() + b * BATCH * pb, BATCH, MAX_SEQ_LEN,
+                                 wfe.NOALLOC_MAX_DISTANCE, d_dist.data_ptr() + 4 * b * BATCH,
+                                 d_cigar.data_ptr() + b * BATCH * CIGAR_STRIDE, CIGAR_STRIDE,
+                                 d_status.data_ptr() + b * BATCH, stream)
+
+    for i in range(nb):
+        step(i)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(steps):
+        step(i)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    got = (d_dist.cpu().numpy(), d_cigar.view(PAIRS, CIGAR_STRIDE).cpu().numpy(), d_status.cpu().numpy())
+    return {"value": steps * BATCH / (ms / 1e3), "unit": "alignments/s", "ms_per_step": ms / steps,
+            "max_distance": wfe.NOALLOC_MAX_DISTANCE, "same_as_context_path": parity(got, want)["mismatches"] == 0,
+            "note": "no context and no allocation: the tier-3 kernel with its backtrace scratch in a fixed "
+                    "16 MiB device array (204 CTAs at most), one call per batch"}
+
+
+def reference_check_baseline(ascii, pairs, cigars) -> dict | None:
+    """The reference's own host check path (Cigars::check_cigar,
+    src/wavefront.cuh:297-419, compiled from the reference's files into
+    oracle/_ref) over every pair's CIGAR, on 1 thread and on every host core
+    (contiguous shares, as src/aligner.cu:45-48 splits pairs).  A validity
+    replay, not an aligner.  None where the library could not be built."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    if not oracle.ref_available():
+        return None
+    import ref_check_baseline as rcb
+    try:
+        recs = rcb.run(ascii, pairs, cigars)
+    except (OSError, subprocess.CalledProcessError, ValueError):
+        return None
+    best = max(recs, key=lambda r: r["pairs_per_s"])
+    return {"value": best["pairs_per_s"], "unit": "pairs checked/s", "threads": best["threads"],
+            "by_threads": {str(r["threads"]): round(r["pairs_per_s"]) for r in recs},
+            "valid": best["valid"], "pairs": best["pairs"], "cores": os.cpu_count(),
+            "kind": "reference Cigars::check_cigar (src/wavefront.cuh:297-419) built from its sources, "
+                    "best of 3; a validity replay of the CIGARs, not an aligner"}
 
 
 def run_reference(args):
@@ -720,9 +1045,8 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "alignments/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-        "data": "synthetic (seeded generator)",
-        "config": {"workload": WORKLOAD, "pairs": PAIRS, "batch": BATCH, "length": LENGTH, "edit_prob": EDIT_P,
-                   "seed": SEED},
+        "data": "synthetic (seeded generator; no dataset)",
+        "config": workload_config(world, len(ascii)),
         "cpu_baseline": {"value": value, "unit": "alignments/s", "cores": nthreads, "kind": "port",
                          "sample": f"{args.steps} batches of {BATCH:,} pairs, {nthreads} threads; the CPU "
                                    "restatement of the reference's kernels (the reference has no CPU aligner)"},
@@ -808,6 +1132,7 @@ def main():
     cg = d_cigar.view(PAIRS, CIGAR_STRIDE).cpu().numpy()
     st_h = d_status.cpu().numpy()
     assert (st_h == 0).all(), "non-OK pair status in the benchmark workload"
+    dev_out = (d_dist.cpu().numpy(), cg, st_h)
     clen = np.minimum(cigar_lengths(cg) + 1, CIGAR_STRIDE)
     bytes_per_batch = []
     for b in range(nb):
@@ -819,7 +1144,9 @@ def main():
     top = int(np.argmax(tier_ms))
     launch_ms = tier_ms[top] / max(1, st["tier_launches"][top])
     peak, peak_kind = measured_hbm_peak()
-    achieved = alg_bytes / (launch_ms / 1e3) / 1e9
+    # one tier-0 launch per step; consecutive launches overlap on two
+    # streams, so the time a launch takes of the step is the time per step
+    achieved = alg_bytes / (ms_max / args.steps / 1e3) / 1e9
     traffic = profiled_traffic()
     gpu_launches = int(st["kernel_launches"])
 
@@ -864,18 +1191,40 @@ def main():
                         "over NVLink-C2C" if in_place else "staged cudaMemcpyAsync copies")}
     if not (np.array_equal(h_dist, d_dist.cpu().numpy())):
         raise SystemExit("host-buffer and device-buffer results differ")
+    e2e_out = (h_dist.copy(), h_cigar.copy(), h_status.copy())
     e2e["pageable"] = pageable_e2e(ascii, pairs, reps, local, world, device, h_dist)
     e2e["link_roofline"] = link_roofline(h2d * reps * nb / e2e_s)
 
+    short = LENGTH == 150
+    noalloc = noalloc_throughput(d_ascii, d_pairs, dev_out, stream, args.steps) if rank == 0 and short else None
+
     base = None
-    ref_cuda = None
+    ref_cuda = cli = ref_check = None
+    checked = None
     int_peak = int32_peak(local) if rank == 0 else None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        base = cpu_baseline(ascii, pairs, os.cpu_count() or 1)
-        ref_cuda = reference_cuda_baseline()
+        base, want = cpu_baseline(ascii, pairs, os.cpu_count() or 1)
+        checked = {"value": parity(dev_out, want), "e2e": parity(e2e_out, want),
+                   "against": "the CPU restatement of the reference (oracle/) on every pair of the workload"}
+        if checked["value"]["mismatches"] or checked["e2e"]["mismatches"]:
+            print(json.dumps({"parity": checked}), file=sys.stderr)
+            raise SystemExit("the timed results differ from the oracle's")
+        if short:
+            ref_check = reference_check_baseline(ascii, pairs, want[1])
+        del want
+        if short:
+            ref_cuda = reference_cuda_baseline()
+            cli = cli_wall()
     int_roof = int_roofline(base, int_peak, ms_max / args.steps, BATCH)
     if base:
         base = {k: v for k, v in base.items() if k != "counts"}
+    versus = None
+    if ref_cuda:
+        versus = {"definition": "this build's time over the reference CUDA build's on the same region",
+                  "e2e_over_ref_steady": e2e["value"] / ref_cuda["steady"]["value"],
+                  "value_over_ref_steady": value / ref_cuda["steady"]["value"]}
+        if cli:
+            versus["cli_over_ref_wall"] = cli["value"] / ref_cuda["value"]
 
     if rank == 0:
         line = {
@@ -883,11 +1232,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic (seeded generator; no dataset)",
-            "config": {"workload": WORKLOAD, "pairs_per_gpu": PAIRS, "batch": BATCH, "length": LENGTH,
-                       "edit_prob": EDIT_P, "seed": SEED, "cigar_stride": CIGAR_STRIDE,
-                       "l2": (f"inputs larger than L2: steps cycle over {nb} batches "
-                              f"({len(ascii) / 1e6:.0f} MB ASCII, {PAIRS * CIGAR_STRIDE / 1e6:.0f} MB CIGAR slots)"),
-                       "parallelism": f"replicas x{world}"},
+            "config": workload_config(world, len(ascii)),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "integer_pipes": {"alu_pipe_pct_of_peak": profiled("alu_pipe_pct_of_peak"),
@@ -897,22 +1242,33 @@ def main():
                          "kernel": f"tier_kernel tier {top}" + (" and the tiers it hands pairs on to (one timed "
                                                                      "chain)" if any(st["tier_passed"]) else ""),
                          "alg_bytes_per_launch": alg_bytes,
-                         "launch_ms": launch_ms,
-                         "achieved_per_step": alg_bytes / (ms_max / args.steps / 1e3) / 1e9,
-                         "overlap": "a call's batches alternate between two streams, so one batch's tier-0 "
-                                    "launch overlaps the next: achieved divides by the launch's own duration, "
-                                    "achieved_per_step by the time per batch of the timed region",
+                         "ms_per_launch": ms_max / args.steps,
+                         "overlap": "one tier-0 launch per step; a call's batches alternate between two streams, "
+                                    "so consecutive launches overlap and the time per step is the time a launch "
+                                    f"adds (each launch spans {launch_ms:.3f} ms from start to end, events on "
+                                    "its stream, while sharing the GPU with its neighbours)",
                          "int32": int_roof},
             "gcups": {"value": value * cells_per_pair / 1e9,
                       "definition": "equivalent DP cell updates: sum of p_len * t_len per second / 1e9"},
             "cpu_baseline": base,
+            "parity": checked,
             "ref_cuda": ref_cuda,
+            "cli": cli,
+            "versus_ref_cuda": versus,
+            "ref_check": ref_check,
+            "noalloc": noalloc,
             "e2e": e2e,
             "gpu_launches": gpu_launches,
             "clocks": clocks.summary(),
             "tiers": {"launches": st["tier_launches"][:7], "ms": [round(x, 4) for x in tier_ms[:7]],
                       "passed_on": st["tier_passed"][:7]},
         }
+        if short and world == 1 and not args.no_cpu_baseline and not args.no_other_workloads:
+            ctx.close()
+            ctx2.close()
+            del d_ascii, d_pairs, d_dist, d_cigar, d_status
+            torch.cuda.empty_cache()
+            line["other_workloads"] = run_other_workloads()
         print(json.dumps(line))
     ctx.close()
     ctx2.close()

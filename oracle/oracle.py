@@ -22,7 +22,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libwfe_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libwfe_ref.so")
-REF_SRC = "/root/reference"
+# the reference checkout, where it is mounted; else the copies of the few files
+# the CPU build needs, staged into _ref/ (never committed) by `make ref-stage`
+REF_SRC = os.environ.get("WFE_REFERENCE_DIR", "/root/reference")
+REF_STAGED = os.path.join(HERE, "_ref", "reference")
 
 OP_INS, OP_SUB, OP_DEL = 1, 2, 3
 PAIR_OK, PAIR_OVER_MAX, PAIR_CIGAR_TRUNCATED = 0, 1, 2
@@ -35,12 +38,17 @@ REF_HARNESS = os.path.join(HERE, "_build", "ref_cuda_harness")
 def build(ref: bool | None = None) -> None:
     """Compile the restatement and the driver of the reference's GPU kernels;
     where the reference sources exist, also the reference-on-CPU library and
-    the reference's kernels as an sm_100 cubin."""
+    the reference's kernels as an sm_100 cubin, and stage the files the CPU
+    library needs into _ref/reference.  Where only that staged copy exists
+    (a machine without the reference, e.g. the GPU machine), the CPU library is
+    built from it."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    if ref is None:
-        ref = os.path.isdir(os.path.join(REF_SRC, "src"))
-    if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", "ref-cubin", f"REF={REF_SRC}"], check=True)
+    mounted = os.path.isdir(os.path.join(REF_SRC, "src"))
+    staged = os.path.isdir(os.path.join(REF_STAGED, "src"))
+    if ref is not False and mounted:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "ref-cubin", "ref-stage", f"REF={REF_SRC}"], check=True)
+    elif ref is not False and staged:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_STAGED}"], check=bool(ref))
     if os.path.exists(REF_CUBIN):
         subprocess.run(["make", "-s", "-C", HERE, "ref-harness"], check=False)
 
@@ -50,15 +58,46 @@ def ref_cuda_available() -> bool:
 
 
 def ref_cuda_run(n: int, length: int, p: float, seed: int, batch: int | None = None, threads: int = 1,
-                 reps: int = 1, dump: str | None = None) -> dict:
+                 reps: int = 1, dump: str | None = None, steady: bool = False) -> dict:
     """Run the reference's own GPU kernels (sm_100 cubin) through the
-    restated batch loop; returns the harness's JSON record."""
+    restated batch loop; returns the harness's JSON record.  steady: the
+    allocations are made before the clock starts and freed after it stops
+    (the batch loop alone is timed)."""
     import json
     cmd = [REF_HARNESS, "--cubin", REF_CUBIN, "-n", str(n), "-l", str(length), "-b", str(batch or n),
            "-t", str(threads), "--p", str(p), "--seed", str(seed), "--reps", str(reps)]
     if dump:
         cmd += ["--dump", dump]
+    if steady:
+        cmd += ["--steady"]
     out = subprocess.run(cmd, check=True, stdout=subprocess.PIPE, text=True).stdout
+    return json.loads(out.strip().splitlines()[-1])
+
+
+def ref_cuda_run_pairs(ascii: np.ndarray, pairs: np.ndarray, slot_len: int, batch: int, threads: int = 1,
+                       reps: int = 1, steady: bool = False, dump: str | None = None) -> dict:
+    """The reference's GPU kernels on given pairs (descriptor records with
+    p_off, p_len, t_off, t_len into `ascii`): written to a pairs file, run
+    with -l slot_len (every sequence at most 2 * slot_len bases)."""
+    import json
+    import tempfile
+    n = len(pairs)
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "pairs.bin")
+        with open(path, "wb") as f:
+            f.write(np.array([n, slot_len], np.uint64).tobytes())
+            f.write(pairs["p_len"].astype(np.uint32).tobytes())
+            f.write(pairs["t_len"].astype(np.uint32).tobytes())
+            for q in pairs:
+                f.write(ascii[q["p_off"]:q["p_off"] + q["p_len"]].tobytes())
+                f.write(ascii[q["t_off"]:q["t_off"] + q["t_len"]].tobytes())
+        cmd = [REF_HARNESS, "--cubin", REF_CUBIN, "--pairs-file", path, "-b", str(min(batch, n)),
+               "-t", str(threads), "--reps", str(reps)]
+        if steady:
+            cmd += ["--steady"]
+        if dump:
+            cmd += ["--dump", dump]
+        out = subprocess.run(cmd, check=True, stdout=subprocess.PIPE, text=True).stdout
     return json.loads(out.strip().splitlines()[-1])
 
 

@@ -25,6 +25,8 @@ static void* run(void* a) { job_t* j = a; size_t g = 0;
 static double now(void) { struct timespec t; clock_gettime(CLOCK_MONOTONIC, &t); return t.tv_sec + 1e-9 * t.tv_nsec; }
 int main(int argc, char** argv) {
   const char* path = argv[1]; size_t n = strtoull(argv[2], 0, 10); int T = atoi(argv[3]);
+  if (T < 1) T = 1;
+  if (T > 64) T = 64; /* the thread arrays below */
   /* raw file: n pairs as u32 plen, u32 tlen, then bytes; produced by the Python driver */
   FILE* f = fopen(path, "rb"); size_t unp = 304, S = 152;
   char* buf = calloc(2 * unp * n + 64, 1); uint32_t* pl = malloc(4 * n); uint32_t* tl = malloc(4 * n);

@@ -20,10 +20,18 @@
  * The module is loaded before the clock starts.
  *
  *   ref_cuda_harness --cubin F -n N -l L [-b B] [-t T] [--p P] [--seed S]
- *                    [--reps R] [--dump FILE]
+ *                    [--reps R] [--dump FILE] [--steady] [--pairs-file F]
  * prints one JSON line: wall time of the timed region (src/aligner.cu:198-233)
  * and alignments per second; --dump writes every CIGAR slot (cigar_max_len
- * bytes per pair, pair order) for parity checks.
+ * bytes per pair, pair order) for parity checks.  --steady times the batch
+ * loop alone: every thread makes its allocations (the Sequences constructor
+ * and the cudaMalloc/cudaMemset of GPU_memory_init) before the clock starts
+ * and frees them after it stops; the clock covers the first batch's copy and
+ * packing, every batch and the last CIGAR copy.  --pairs-file aligns given
+ * pairs instead of generated ones: a u64 pair count n, a u64 slot length l
+ * (the reader's -l: every sequence at most 2*l bases), u32 pattern lengths
+ * [n], u32 text lengths [n], then each pair's pattern and text bytes; -n and
+ * -l come from the file.
  */
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -96,7 +104,12 @@ struct Params {                    /* src/aligner.cu:29-38 */
     unsigned tid, total_threads;
     const Reader* reader;
     signed char* dump;
+    pthread_barrier_t* steady;     /* --steady: threads meet after allocating and before freeing */
+    double* t_start;               /* --steady: the clock, read by thread 0 at the meetings */
+    double* t_stop;
 };
+
+double now_s();
 
 void launch(CUfunction f, unsigned gx, unsigned bx, unsigned by, unsigned smem, CUstream s, void** args)
 {
@@ -136,6 +149,12 @@ struct Sequences {
 
     void GPU_memory_init() /* src/wavefront.cu:29-108 */
     {
+        GPU_memory_alloc();
+        GPU_memory_first_batch();
+    }
+
+    void GPU_memory_alloc() /* src/wavefront.cu:29-70: the allocations */
+    {
         CK(cudaMalloc((void**)&d_elements, pad * sizeof(WF_element)));
         CK(cudaMemset(d_elements, 0, pad * sizeof(WF_element)));
         const size_t packed = r->max_seq_len;
@@ -143,6 +162,11 @@ struct Sequences {
         CK(cudaMemset(seq_dev, 0, packed * 2 * batch_size));
         const size_t unp = r->max_seq_len_unpacked;
         CK(cudaMalloc((void**)&seq_dev_unpacked, unp * 2 * batch_size));
+    }
+
+    void GPU_memory_first_batch() /* src/wavefront.cu:71-108: first copy, packing, elements */
+    {
+        const size_t unp = r->max_seq_len_unpacked;
         const char* first = r->sequences_mem_unpacked + unp * 2 * initial_alignment;
         CK(cudaMemcpy(seq_dev_unpacked, first, unp * 2 * batch_size, cudaMemcpyHostToDevice));
         const unsigned bx = (unsigned)std::min<size_t>(r->seq_len / 4, 256);
@@ -233,10 +257,22 @@ void* worker(void* arg) /* src/aligner.cu:40-71 */
     size_t batch = p->batch_size;
     if (batch > n) batch = n;
     Sequences s(p->reader->sequences, n, p->seq_len, batch, p->reader, (int)skip, p->dump);
-    s.GPU_memory_init();
+    if (p->steady) {
+        s.GPU_memory_alloc();
+        CK(cudaDeviceSynchronize());
+        pthread_barrier_wait(p->steady);
+        if (p->tid == 0) *p->t_start = now_s();
+        s.GPU_memory_first_batch();
+    } else {
+        s.GPU_memory_init();
+    }
     do {
         s.GPU_launch_wavefront_distance();
     } while (s.prepare_next_batch());
+    if (p->steady) {
+        pthread_barrier_wait(p->steady);
+        if (p->tid == 0) *p->t_stop = now_s();
+    }
     s.GPU_memory_free();
     return nullptr;
 }
@@ -256,6 +292,8 @@ int main(int argc, char** argv)
     const char* dump_path = nullptr;
     size_t n = 0, l = 0, b = 0;
     unsigned threads = 1, reps = 1;
+    bool steady = false;
+    const char* pairs_path = nullptr;
     double prob = 0.05;
     unsigned long long seed = 2;
     for (int i = 1; i < argc; ++i) {
@@ -270,7 +308,24 @@ int main(int argc, char** argv)
         else if (!strcmp(a, "--seed")) { seed = strtoull(v, nullptr, 10); ++i; }
         else if (!strcmp(a, "--reps")) { reps = (unsigned)atoi(v); ++i; }
         else if (!strcmp(a, "--dump")) { dump_path = v; ++i; }
+        else if (!strcmp(a, "--steady")) { steady = true; }
+        else if (!strcmp(a, "--pairs-file")) { pairs_path = v; ++i; }
         else { fprintf(stderr, "unknown argument %s\n", a); return 1; }
+    }
+    FILE* pf = nullptr;
+    std::vector<uint32_t> fpl, ftl;
+    if (pairs_path) {
+        pf = fopen(pairs_path, "rb");
+        uint64_t hdr[2];
+        if (!pf || fread(hdr, 8, 2, pf) != 2) { fprintf(stderr, "cannot read %s\n", pairs_path); return 1; }
+        n = (size_t)hdr[0];
+        l = (size_t)hdr[1];
+        fpl.resize(n);
+        ftl.resize(n);
+        if (fread(fpl.data(), 4, n, pf) != n || fread(ftl.data(), 4, n, pf) != n) {
+            fprintf(stderr, "short pairs file\n");
+            return 1;
+        }
     }
     if (!cubin || !n || !l) {
         fprintf(stderr, "usage: %s --cubin F -n N -l L [-b B] [-t T] [--p P] [--seed S] [--reps R] [--dump F]\n", argv[0]);
@@ -294,7 +349,19 @@ int main(int argc, char** argv)
     std::vector<char> pat(2 * l + 1), txt(l + 1);
     for (size_t i = 0; i < n; ++i) {
         uint32_t pl, tl;
-        wfe_gen_pair(&gc, i, pat.data(), &pl, txt.data(), &tl);
+        if (pf) {
+            pl = fpl[i];
+            tl = ftl[i];
+            if (pl > 2 * l || tl > 2 * l) { fprintf(stderr, "pair too long\n"); return 1; }
+            if (pat.size() < pl + 1u) pat.resize(pl + 1u);
+            if (txt.size() < tl + 1u) txt.resize(tl + 1u);
+            if (fread(pat.data(), 1, pl, pf) != pl || fread(txt.data(), 1, tl, pf) != tl) {
+                fprintf(stderr, "short pairs file\n");
+                return 1;
+            }
+        } else {
+            wfe_gen_pair(&gc, i, pat.data(), &pl, txt.data(), &tl);
+        }
         if (pl > r.max_seq_len_unpacked || tl > r.max_seq_len_unpacked) { fprintf(stderr, "pair too long\n"); return 1; }
         memcpy(r.sequences_mem_unpacked + 2 * i * r.max_seq_len_unpacked, pat.data(), pl);
         memcpy(r.sequences_mem_unpacked + (2 * i + 1) * r.max_seq_len_unpacked, txt.data(), tl);
@@ -303,6 +370,7 @@ int main(int argc, char** argv)
         r.sequences[i].tlen = tl;
     }
 
+    if (pf) fclose(pf);
     CK(cudaFree(nullptr)); /* primary context */
     CKD(cuInit(0));
     CUmodule mod;
@@ -320,13 +388,21 @@ int main(int argc, char** argv)
     for (unsigned rep = 0; rep < reps; ++rep) {
         std::vector<pthread_t> th(threads);
         std::vector<Params> ps(threads);
+        pthread_barrier_t bar;
+        double ts = 0, te = 0;
+        if (steady) pthread_barrier_init(&bar, nullptr, threads);
         const double t0 = now_s(); /* CLOCK_START_NO_DEBUG, src/aligner.cu:198-199 */
         for (unsigned t = 0; t < threads; ++t)
-            ps[t] = Params{l, n, b, t, threads, &r, dump_path ? dump.data() : nullptr};
+            ps[t] = Params{l, n, b, t, threads, &r, dump_path ? dump.data() : nullptr, steady ? &bar : nullptr,
+                           &ts, &te};
         for (unsigned t = 1; t < threads; ++t) pthread_create(&th[t], nullptr, worker, &ps[t]);
         worker(&ps[0]);
         for (unsigned t = 1; t < threads; ++t) pthread_join(th[t], nullptr);
-        const double dt = now_s() - t0; /* CLOCK_STOP_NO_DEBUG, src/aligner.cu:233 */
+        double dt = now_s() - t0; /* CLOCK_STOP_NO_DEBUG, src/aligner.cu:233 */
+        if (steady) {
+            dt = te - ts;
+            pthread_barrier_destroy(&bar);
+        }
         best = std::min(best, dt);
         total += dt;
     }
@@ -337,7 +413,7 @@ int main(int argc, char** argv)
         fclose(f);
     }
     printf("{\"impl\": \"reference-cuda-sm100\", \"n\": %zu, \"l\": %zu, \"b\": %zu, \"t\": %u, \"reps\": %u, "
-           "\"best_wall_s\": %.6f, \"mean_wall_s\": %.6f, \"alignments_per_s\": %.1f}\n",
-           n, l, b, threads, reps, best, total / reps, (double)n / best);
+           "\"steady\": %s, \"best_wall_s\": %.6f, \"mean_wall_s\": %.6f, \"alignments_per_s\": %.1f}\n",
+           n, l, b, threads, reps, steady ? "true" : "false", best, total / reps, (double)n / best);
     return 0;
 }

@@ -3,9 +3,9 @@
 Runs the reference's own kernels (src/kernels.cu of quim0/eWFA-GPU, compiled
 for the CPU into oracle/_ref by oracle/Makefile) and its host helpers
 (src/wavefront.cuh) on a fixed set of pairs and stores inputs and outputs in
-ref_vectors.npz.  Needs the reference sources at /root/reference, so it runs
-only where they are mounted; the fixture it writes is committed and is all the
-tests read.
+ref_vectors.npz.  Needs the reference sources (at $WFE_REFERENCE_DIR, else
+/root/reference), so it runs only where they are mounted; the fixture it writes
+is committed and is all the tests read.
 
     python tests/golden/make_golden.py
 
