@@ -636,9 +636,15 @@ def summarise(name: str, d: dict) -> dict:
         rows = [{"load": r["load"], "served": {k: r["served"][k] for k in ("p50_ms", "p99_ms", "alignments_per_s")},
                  "plain": {k: r["plain"][k] for k in ("p50_ms", "p99_ms", "alignments_per_s")}}
                 for r in d["rates"]]
+        srv = d.get("server") or {}
+        nb = max(1, srv.get("batches", 0))
+        sched = {"batches": srv.get("batches"), "admit_us_per_batch": srv.get("admit_ns", 0) / nb / 1e3,
+                 "finish_us_per_batch": srv.get("finish_ns", 0) / nb / 1e3,
+                 "note": "host time of the scheduler thread per batch (forming it, enqueueing copies and kernels; "
+                         "copying results out): what a device-resident request queue could remove"}
         return {"config": d["config"], "peak_alignments_per_s": d["peak_alignments_per_s"], "rates": rows,
                 "identical_results": d["identical_results"], "all_ok": d["all_ok"], "parity": d["parity"],
-                "ref_cuda": d.get("ref_cuda")}
+                "scheduler": sched, "ref_cuda": d.get("ref_cuda")}
     return d
 
 

@@ -159,7 +159,7 @@ int pop_launch_error(wfe_ctx* ctx)
     return fail_cuda(ctx, cudaErrorLaunchFailure);
 }
 
-constexpr size_t kLaunchErrorBytes = 8; /* one byte per tier (kNumTiers <= 8) */
+constexpr size_t kLaunchErrorBytes = 8; /* byte t: a device-side launch of tier t failed */
 static_assert(kNumTiers <= (int)kLaunchErrorBytes, "one launch-error byte per tier");
 
 void free_launch_error(wfe_ctx* ctx)

@@ -413,9 +413,11 @@ void run_scheduler(wfe_server* s)
                 if (q != cudaSuccess && q != cudaErrorNotReady) b->rc = WFE_ERR_CUDA;
                 else b->rc = wfe::take_launch_error(L.ctx);
             }
+            const uint64_t t0 = now_ns();
             scatter(s, b);
             const uint64_t t = now_ns();
             lk.lock();
+            s->stats.finish_ns += t - t0;
             for (const Share& sh : b->shares) {
                 Request* r = sh.r;
                 if (b->rc != WFE_OK) r->rc = b->rc;
@@ -437,16 +439,19 @@ void run_scheduler(wfe_server* s)
         }
         bool launched = false;
         for (;;) {
+            const uint64_t t0 = now_ns();
             Batch* b = form_batch(s);
             if (!b) break;
             lk.unlock();
             b->rc = launch_batch(s, b);
+            const uint64_t t1 = now_ns();
             if (b->rc != WFE_OK) {
                 /* finishes as failed, without results, once what was queued is done */
                 cudaStreamSynchronize(s->lanes[b->lane].stream);
                 batch_done(b);
             }
             lk.lock();
+            s->stats.admit_ns += t1 - t0;
             launched = true;
         }
         if (s->stopping && s->pending.empty() && s->in_flight == 0 && s->finished.empty()) break;

@@ -77,7 +77,8 @@ class RequestInfo(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("requests", C.c_uint64), ("pairs", C.c_uint64), ("batches", C.c_uint64),
                 ("split_requests", C.c_uint64), ("max_in_flight", C.c_uint32), ("lanes", C.c_uint32),
-                ("memory_bytes", C.c_uint64), ("peak_memory", C.c_uint64)]
+                ("memory_bytes", C.c_uint64), ("peak_memory", C.c_uint64), ("admit_ns", C.c_uint64),
+                ("finish_ns", C.c_uint64)]
 
 
 class PairFileC(C.Structure):

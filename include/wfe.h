@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define WFE_ABI_VERSION 1
+#define WFE_ABI_VERSION 2 /* 2: wfe_server_stats gained admit_ns and finish_ns */
 
 /* Call status.  The reference exits the process on any CUDA error
  * (utils/cuda_helpers.cuh:24-31) or fatal condition (utils/logger.h:66-68). */
@@ -389,6 +389,10 @@ typedef struct wfe_server_stats {
     uint32_t lanes;
     uint64_t memory_bytes;    /* arena size */
     uint64_t peak_memory;     /* most arena bytes held at once */
+    uint64_t admit_ns;        /* host time the scheduler spent forming batches and
+                                 enqueueing their copies and kernels */
+    uint64_t finish_ns;       /* host time it spent copying results out and
+                                 finishing requests */
 } wfe_server_stats;
 
 /* Create a server (one context per lane, created with WFE_FLAG_DEVICE_ONLY,
