@@ -265,6 +265,21 @@ __device__ __forceinline__ void pack_from_span(const uint32_t* words, uintptr_t 
     if (g == 0) Q[nw - 1].x = 0u;
 }
 
+/* The best of a cell's three candidates, with the operation in the low two
+ * bits (src/kernels.cu:136-152): deletion from diagonal k+1 (its offset),
+ * mismatch from k (offset + 1), insertion from k-1 (offset + 1); the
+ * largest offset wins and equal offsets go to the larger operation code,
+ * DEL > SUB > INS.  An offset of -1 (outside the previous wavefront) gives a
+ * deletion of -1 and candidates 2 and 1 for the others, as in the
+ * reference.  Written as multiply-adds and one three-way maximum. */
+__device__ __forceinline__ int piggyback_max(int up, int self, int dn)
+{
+    const int del_p = (int)((unsigned)up * 4u + (unsigned)kOpDel);
+    const int sub_p = (int)((unsigned)self * 4u + (unsigned)(4 + kOpSub));
+    const int ins_p = (int)((unsigned)dn * 4u + (unsigned)(4 + kOpIns));
+    return __vimax3_s32(del_p, sub_p, ins_p);
+}
+
 /* 16-base window of a packed sequence starting at base v. */
 __device__ __forceinline__ uint32_t window(const uint2* Q, int v)
 {

@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <map>
 #include <mutex>
+#include <tuple>
 
 namespace wfe {
 
@@ -420,10 +421,7 @@ __device__ __forceinline__ void tier_body(const AlignLaunch& A, uint32_t seq_wor
                     const int dnsrc = (c > 0) ? O[(c > 0) ? c - 1 : 0] : -1;
                     const int up = __shfl_sync(kFull, g == 0 ? upsrc : O[c], (g + 1) & (G - 1), G);
                     const int dn = __shfl_sync(kFull, g == G - 1 ? dnsrc : O[c], (g + G - 1) & (G - 1), G);
-                    const int del_p = (int)(((unsigned)up) << 2) | kOpDel;
-                    const int sub_p = (int)(((unsigned)(O[c] + 1)) << 2) | kOpSub;
-                    const int ins_p = (int)(((unsigned)(dn + 1)) << 2) | kOpIns;
-                    const int m = max(max(del_p, sub_p), ins_p);
+                    const int m = piggyback_max(up, O[c], dn);
                     const unsigned blo = __ballot_sync(kFull, m & 1);
                     const unsigned bhi = __ballot_sync(kFull, m & 2);
                     if (!PREDICT && run && g == 0)
@@ -614,22 +612,23 @@ __global__ void long_kernel(const __grid_constant__ AlignLaunch A)
             int* prev = bufA;
             int* next = bufB;
             if (!(kt == 0 && prev[0] == tlen)) {
+                uint2* row = ops; /* row d of the backtrace store: long_row(d), kept running */
+                /* last step: the tier's limit or the caller's cap */
+                const int dstop = A.max_distance > 0 ? min(dlim, A.max_distance) : dlim;
                 for (int d = 1;; ++d) {
-                    if (A.max_distance > 0 && d > A.max_distance) { state = ST_OVERMAX; break; }
-                    if (d > dlim) { state = ST_OVERFLOW; break; }
+                    if (d > dstop) {
+                        state = (A.max_distance > 0 && d > A.max_distance) ? ST_OVERMAX : ST_OVERFLOW;
+                        break;
+                    }
                     const int ncell = 2 * d + 1;
                     const int nchunk = (ncell + 31) >> 5;
-                    uint2* row = ops + long_row(d);
                     for (int q = warp; q < nchunk; q += kW) {
                         const int i = 32 * q + lane;
                         const int k = i - d;
                         const bool valid = i < ncell;
                         int m = 0;
                         if (valid) {
-                            const int del_p = (int)(((unsigned)prev[k + 1]) << 2) | kOpDel;
-                            const int sub_p = (int)(((unsigned)(prev[k] + 1)) << 2) | kOpSub;
-                            const int ins_p = (int)(((unsigned)(prev[k - 1] + 1)) << 2) | kOpIns;
-                            m = max(max(del_p, sub_p), ins_p);
+                            m = piggyback_max(prev[k + 1], prev[k], prev[k - 1]);
                             next[k] = extend_lane(QP, QT, plen, tlen, k, m >> 2);
                         }
                         const unsigned lo = __ballot_sync(kFull, m & 1);
@@ -640,6 +639,7 @@ __global__ void long_kernel(const __grid_constant__ AlignLaunch A)
                     __syncthreads();
                     if (kt >= -d && kt <= d && next[kt] == tlen) { D = d; break; }
                     int* t = prev; prev = next; next = t;
+                    row += nchunk;
                 }
             }
             if (state == ST_RUN) state = ST_DONE;
@@ -1025,7 +1025,9 @@ cudaError_t launch_long(const AlignLaunch& a, int grid, cudaStream_t s)
 
 }  // namespace
 
-TierShape tier_shape(int tier, uint32_t max_len, uint32_t cigar_stride, int sm_count)
+namespace {
+
+TierShape compute_tier_shape(int tier, uint32_t max_len, uint32_t cigar_stride, int sm_count)
 {
     switch (tier) {
     case 0: return shape_of<T0>(max_len, cigar_stride, sm_count);
@@ -1037,6 +1039,27 @@ TierShape tier_shape(int tier, uint32_t max_len, uint32_t cigar_stride, int sm_c
     case 6: return max_len > (uint32_t)kLongSmemDistance ? long_shape_of<true>(max_len, sm_count) : TierShape{};
     default: return TierShape{};
     }
+}
+
+}  // namespace
+
+/* Shapes depend only on the device and the arguments; each occupancy query
+ * costs tens of microseconds the first time, and a context asks for every
+ * tier's shape at creation and again for its first bucket, so results are
+ * kept per device for the life of the process. */
+TierShape tier_shape(int tier, uint32_t max_len, uint32_t cigar_stride, int sm_count)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return TierShape{};
+    static std::mutex mu;
+    static std::map<std::tuple<int, int, uint32_t, uint32_t, int>, TierShape> known;
+    const auto key = std::make_tuple(dev, tier, max_len, cigar_stride, sm_count);
+    std::lock_guard<std::mutex> lock(mu);
+    const auto it = known.find(key);
+    if (it != known.end()) return it->second;
+    const TierShape sh = compute_tier_shape(tier, max_len, cigar_stride, sm_count);
+    known.emplace(key, sh);
+    return sh;
 }
 
 int tier_grid(int tier, uint32_t max_len, uint32_t cigar_stride, int sm_count)
