@@ -59,37 +59,16 @@ enum : int { ST_IDLE = 0, ST_RUN, ST_DONE, ST_OVERFLOW, ST_OVERMAX, ST_TOOLONG, 
 
 __host__ __device__ constexpr size_t round16(size_t x) { return (x + 15u) & ~size_t(15); }
 
-/* 2 bits per diagonal for the G diagonals of one chunk: the low bits of the
- * operations, then the high bits. */
-template <int G> struct OpEntry;
-template <> struct OpEntry<4> {
-    using T = uint8_t;
-    static __device__ __forceinline__ void put(T* p, int i, uint32_t lo, uint32_t hi)
-    { p[i] = (T)(lo | (hi << 4)); }
-    static __device__ __forceinline__ int get(const T* p, int i, int gl)
-    { const uint32_t e = p[i]; return (int)(((e >> gl) & 1u) | (((e >> (4 + gl)) & 1u) << 1)); }
-};
-template <> struct OpEntry<8> {
-    using T = uint16_t;
-    static __device__ __forceinline__ void put(T* p, int i, uint32_t lo, uint32_t hi)
-    { p[i] = (T)(lo | (hi << 8)); }
-    static __device__ __forceinline__ int get(const T* p, int i, int gl)
-    { const uint32_t e = p[i]; return (int)(((e >> gl) & 1u) | (((e >> (8 + gl)) & 1u) << 1)); }
-};
-template <> struct OpEntry<16> {
-    using T = uint32_t;
-    static __device__ __forceinline__ void put(T* p, int i, uint32_t lo, uint32_t hi)
-    { p[i] = lo | (hi << 16); }
-    static __device__ __forceinline__ int get(const T* p, int i, int gl)
-    { const uint32_t e = p[i]; return (int)(((e >> gl) & 1u) | (((e >> (16 + gl)) & 1u) << 1)); }
-};
-template <> struct OpEntry<32> {
-    using T = uint2;
-    static __device__ __forceinline__ void put(T* p, int i, uint32_t lo, uint32_t hi)
-    { p[i] = make_uint2(lo, hi); }
-    static __device__ __forceinline__ int get(const T* p, int i, int gl)
-    { const uint2 e = p[i]; return (int)(((e.x >> gl) & 1u) | (((e.y >> gl) & 1u) << 1)); }
-};
+/* Backtrace store entry of one chunk of one score step: the two ballots of
+ * the warp -- the low and the high bits of the 2-bit operation of every lane's
+ * diagonal -- written by lane 0.  Group grp's diagonal g of the chunk is bit
+ * grp * G + g.  A warp of several groups (G < 32) keeps one store for all of
+ * them, so the ballots are stored as they come, with no per-group shifting and
+ * masking in the score loop; the backtrace picks its group's bits. */
+__device__ __forceinline__ int op_of(uint2 e, int bit)
+{
+    return (int)(((e.x >> bit) & 1u) | (((e.y >> bit) & 1u) << 1));
+}
 
 /* One distance tier: G lanes per pair, 2J+1 register chunks, backtrace
  * store in shared (SMEM_OPS) or global memory, sequences of up to RMAX*G
@@ -102,8 +81,6 @@ struct Tier {
     static constexpr int NC = 2 * J + 1;
     static constexpr int DCAP = G * J + G / 2 - 1;
     static constexpr int GPW = 32 / G;
-    using OE = OpEntry<G>;
-    using E = typename OE::T;
     /* Row d of the backtrace store.  The 32-lane tiers keep only the chunks
      * that score step d touches -- the contiguous range whose diagonals meet
      * [-d, d] -- row after row (a triangle, 55-68 % of DCAP x NC entries),
@@ -128,11 +105,14 @@ struct Tier {
         for (int d = 1; d <= rows && d <= DCAP; ++d) t += row_entries(d);
         return t;
     }
-    static constexpr size_t ops_bytes = round16(sizeof(E) * (size_t)store_entries());
-    /* one group's store for distances up to max_len */
+    /* a group's share of its warp's store (one 8-byte entry per chunk and
+     * score step, shared by the warp's GPW groups) */
+    static constexpr size_t ops_bytes = round16((8u * (size_t)store_entries() + GPW - 1) / GPW);
+    /* one group's store in global scratch (the 32-lane tiers: one group per
+     * warp) for distances up to max_len */
     static size_t store_bytes(uint32_t max_len)
     {
-        return round16(sizeof(E) * (size_t)store_entries((int)std::min<uint32_t>(max_len, (uint32_t)DCAP)));
+        return round16(8u * (size_t)store_entries((int)std::min<uint32_t>(max_len, (uint32_t)DCAP)));
     }
     static int store_rows(uint32_t max_len) { return (int)std::min<uint32_t>(max_len, (uint32_t)DCAP); }
     static constexpr size_t chain_bytes = round16((size_t)DCAP + 1);
@@ -142,9 +122,11 @@ struct Tier {
 inline uint32_t seq_words_for(uint32_t max_len) { return std::max<uint32_t>(1u, (max_len + 15u) / 16u); }
 
 /* Shared memory of one group: both sequences, the operation chain, then one
- * region that first holds the backtrace store (when it lives in shared
- * memory) and, once the chain has been read from it, the CIGAR stage and the
- * runs of the replay. */
+ * region that first holds the group's share of its warp's backtrace store
+ * (when it lives in shared memory) and, once the chains have been read from
+ * it, the group's CIGAR stage and the runs of the replay.  Within a warp's
+ * block the groups' sequences and chains come first, then their union
+ * regions one after another, which together hold the warp's store. */
 template <class T>
 size_t union_bytes(uint32_t cigar_stride)
 {
@@ -312,32 +294,34 @@ template <class T, bool PREDICT>
 __device__ __forceinline__ void tier_body(const AlignLaunch& A, uint32_t seq_words, uint32_t gbytes)
 {
     constexpr int G = T::G, J = T::J, NC = T::NC, DCAP = T::DCAP, GPW = T::GPW;
-    using OE = typename T::OE;
-    using E = typename T::E;
     extern __shared__ __align__(16) unsigned char smem[];
 
     const int lane = (int)(threadIdx.x & 31u), warp = (int)(threadIdx.x >> 5);
     const int g = lane & (G - 1), grp = lane / G;
     const unsigned gmask = (G == 32) ? kFull : (((1u << (G & 31)) - 1u) << (grp * G));
-    const uint32_t gbits = (G == 32) ? kFull : ((1u << (G & 31)) - 1u);
     const int slot = warp * GPW + grp;
 
-    unsigned char* gs = smem + (size_t)slot * gbytes;
+    /* the warp's block: GPW x (sequences, chain), then GPW union regions */
+    const size_t seqchain = 16u * (size_t)seq_words + T::chain_bytes;
+    unsigned char* wblock = smem + (size_t)warp * GPW * gbytes;
+    unsigned char* gs = wblock + (size_t)grp * seqchain;
     uint2* QP = reinterpret_cast<uint2*>(gs);
     uint2* QT = QP + seq_words;
     uint8_t* chain = gs + 16u * (size_t)seq_words;
-    unsigned char* uni = chain + T::chain_bytes;
-    E* ops;
+    unsigned char* unis = wblock + (size_t)GPW * seqchain;
+    unsigned char* uni = unis + (size_t)grp * (gbytes - seqchain);
+    uint2* ops;
     /* last score step the backtrace store holds: a pair that would go past
      * it (never expected: a distance is at most the longest sequence, and
      * the store holds that many rows) goes on to the next tier instead */
     int store_last = DCAP;
     if constexpr (T::SMEM_OPS) {
-        ops = reinterpret_cast<E*>(uni);
+        ops = reinterpret_cast<uint2*>(unis);
     } else {
+        static_assert(T::SMEM_OPS || GPW == 1, "a store in global scratch belongs to one group");
         const TierShape& tsh = A.chain.shape[A.tier];
         const size_t gslot = (size_t)blockIdx.x * (kWarps * GPW) + (size_t)slot;
-        ops = reinterpret_cast<E*>(A.ops_scratch + gslot * tsh.ops_group_bytes);
+        ops = reinterpret_cast<uint2*>(A.ops_scratch + gslot * tsh.ops_group_bytes);
         store_last = min(DCAP, tsh.ops_rows);
     }
     int8_t* stage = reinterpret_cast<int8_t*>(uni);
@@ -424,9 +408,7 @@ __device__ __forceinline__ void tier_body(const AlignLaunch& A, uint32_t seq_wor
                     const int m = piggyback_max(up, O[c], dn);
                     const unsigned blo = __ballot_sync(kFull, m & 1);
                     const unsigned bhi = __ballot_sync(kFull, m & 2);
-                    if (!PREDICT && run && g == 0)
-                        OE::put(ops, rowbase + c - clo, (blo >> ((grp * G) & 31)) & gbits,
-                                (bhi >> ((grp * G) & 31)) & gbits);
+                    if (!PREDICT && lane == 0) ops[rowbase + c - clo] = make_uint2(blo, bhi);
                     const int k = lo_k + g;
                     N[c] = (run && k >= -d && k <= d) ? (m >> 2) : -1;
                 }
@@ -467,7 +449,7 @@ __device__ __forceinline__ void tier_body(const AlignLaunch& A, uint32_t seq_wor
                 for (int s = D; s >= 1; --s) {
                     if (k < -s || k > s) { walk_ok = 0; break; }
                     const int idx = k + G / 2 + G * J;
-                    const int op = OE::get(ops, row + idx / G - T::chunk_lo(s), idx & (G - 1));
+                    const int op = op_of(ops[row + idx / G - T::chunk_lo(s)], grp * G + (idx & (G - 1)));
                     chain[s - 1] = (uint8_t)op;
                     k += op - 2;
                     if (s > 1) row -= T::row_entries(s - 1);
@@ -477,6 +459,9 @@ __device__ __forceinline__ void tier_body(const AlignLaunch& A, uint32_t seq_wor
             walk_ok = __shfl_sync(gmask, walk_ok, 0, G);
             if (!walk_ok) state = ST_BADWALK;
         }
+        /* the warp's store is read by every group's walk before any group's
+         * replay reuses its union region */
+        if constexpr (T::SMEM_OPS && GPW > 1) __syncwarp();
         if (state == ST_DONE) {
             __syncwarp(gmask);
             const int len = replay_chain<G>(QP, QT, plen, tlen, chain, D, runs, stage, A.cigar_stride,
