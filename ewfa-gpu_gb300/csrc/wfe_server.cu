@@ -21,9 +21,11 @@
  *             block of both arenas and `batch_pairs`; a request that does
  *             not fit whole is split, its remaining pairs leading the next
  *             batch;
- *   results   a host function queued behind each batch wakes the scheduler,
- *             which copies every request's share of the results into the
- *             caller's buffers and finishes the requests that are complete.
+ *   results   a host function queued behind each batch wakes one of up to
+ *             four finisher threads, which copies every request's share of
+ *             the results into the caller's buffers, finishes the requests
+ *             that are complete and frees the batch's lane, while the
+ *             scheduler goes on admitting.
  *
  * Sequences reach the device as one copy per request share: the share's
  * span of the caller's buffer when its pairs lie close together (pinned
@@ -177,16 +179,23 @@ struct wfe_server {
     uint64_t host_arena_bytes = 0;
     Arena dev, host;
     std::mutex mu;
-    std::condition_variable cv_work; /* scheduler: requests or finished batches */
-    std::condition_variable cv_done; /* pollers: requests finished */
+    std::condition_variable cv_work;   /* scheduler: requests arrived or a lane came free */
+    std::condition_variable cv_finish; /* finishers: a batch's host function ran */
+    std::condition_variable cv_done;   /* pollers: requests finished */
     std::deque<Request*> pending;
     std::unordered_map<uint64_t, Request*> tickets;
-    std::vector<Batch*> finished;    /* batches whose host function ran */
+    std::deque<Batch*> finished;       /* batches whose host function ran, oldest first */
     uint64_t next_id = 1;
     uint32_t in_flight = 0;
     bool stopping = false;
+    bool finishers_stop = false;
     wfe_server_stats stats{};
     std::thread scheduler;
+    /* Copying a batch's results into the callers' buffers takes several times
+     * as long as admitting one, so it runs on these threads, not on the
+     * scheduler's: the next batch is admitted while the last one's results
+     * are copied out. */
+    std::vector<std::thread> finishers;
 };
 
 namespace {
@@ -233,7 +242,7 @@ void CUDART_CB batch_done(void* arg)
     wfe_server* s = b->srv;
     std::lock_guard<std::mutex> lk(s->mu);
     s->finished.push_back(b);
-    s->cv_work.notify_one();
+    s->cv_finish.notify_one();
 }
 
 /* Take waiting requests into a batch for a free lane (called with the lock
@@ -398,45 +407,66 @@ void scatter(wfe_server* s, Batch* b)
     }
 }
 
+/* A batch whose host function ran: check it, copy its results out (without
+ * the lock: only this thread touches the batch, and its shares' rows of the
+ * callers' buffers belong to no other batch), then finish its requests and
+ * free its lane and arena blocks. */
+void finish_batch(wfe_server* s, Batch* b)
+{
+    Lane& L = s->lanes[b->lane];
+    if (b->rc == WFE_OK) {
+        /* the lane is busy until this batch is finished: no other thread
+         * uses its context now */
+        const cudaError_t q = cudaStreamQuery(L.stream);
+        if (q != cudaSuccess && q != cudaErrorNotReady) b->rc = WFE_ERR_CUDA;
+        else b->rc = wfe::take_launch_error(L.ctx);
+    }
+    const uint64_t t0 = now_ns();
+    scatter(s, b);
+    const uint64_t t = now_ns();
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stats.finish_ns += t - t0;
+    for (const Share& sh : b->shares) {
+        Request* r = sh.r;
+        if (b->rc != WFE_OK) r->rc = b->rc;
+        r->finished += sh.count;
+        if (r->finished == r->n) {
+            r->done = true;
+            r->done_ns = t;
+            s->stats.requests++;
+            s->stats.pairs += r->n;
+            if (r->batches > 1) s->stats.split_requests++;
+        }
+    }
+    s->dev.release(b->dev_off, b->dev_bytes);
+    s->host.release(b->host_off, b->host_bytes);
+    L.busy = false;
+    s->in_flight--;
+    delete b;
+    s->cv_done.notify_all();
+    s->cv_work.notify_one();
+}
+
+void run_finisher(wfe_server* s)
+{
+    cudaSetDevice(s->cfg.device);
+    std::unique_lock<std::mutex> lk(s->mu);
+    for (;;) {
+        s->cv_finish.wait(lk, [s] { return !s->finished.empty() || s->finishers_stop; });
+        if (s->finished.empty()) break; /* stopping, and nothing left */
+        Batch* b = s->finished.front();
+        s->finished.pop_front();
+        lk.unlock();
+        finish_batch(s, b);
+        lk.lock();
+    }
+}
+
 void run_scheduler(wfe_server* s)
 {
     cudaSetDevice(s->cfg.device);
     std::unique_lock<std::mutex> lk(s->mu);
     for (;;) {
-        while (!s->finished.empty()) {
-            Batch* b = s->finished.back();
-            s->finished.pop_back();
-            lk.unlock();
-            Lane& L = s->lanes[b->lane];
-            if (b->rc == WFE_OK) {
-                const cudaError_t q = cudaStreamQuery(L.stream);
-                if (q != cudaSuccess && q != cudaErrorNotReady) b->rc = WFE_ERR_CUDA;
-                else b->rc = wfe::take_launch_error(L.ctx);
-            }
-            const uint64_t t0 = now_ns();
-            scatter(s, b);
-            const uint64_t t = now_ns();
-            lk.lock();
-            s->stats.finish_ns += t - t0;
-            for (const Share& sh : b->shares) {
-                Request* r = sh.r;
-                if (b->rc != WFE_OK) r->rc = b->rc;
-                r->finished += sh.count;
-                if (r->finished == r->n) {
-                    r->done = true;
-                    r->done_ns = t;
-                    s->stats.requests++;
-                    s->stats.pairs += r->n;
-                    if (r->batches > 1) s->stats.split_requests++;
-                }
-            }
-            s->dev.release(b->dev_off, b->dev_bytes);
-            s->host.release(b->host_off, b->host_bytes);
-            L.busy = false;
-            s->in_flight--;
-            delete b;
-            s->cv_done.notify_all();
-        }
         bool launched = false;
         for (;;) {
             const uint64_t t0 = now_ns();
@@ -454,9 +484,22 @@ void run_scheduler(wfe_server* s)
             s->stats.admit_ns += t1 - t0;
             launched = true;
         }
-        if (s->stopping && s->pending.empty() && s->in_flight == 0 && s->finished.empty()) break;
-        if (!launched && s->finished.empty()) s->cv_work.wait(lk);
+        if (s->stopping && s->pending.empty() && s->in_flight == 0) break;
+        if (!launched) s->cv_work.wait(lk);
     }
+}
+
+/* Stop the finishers (after the scheduler: every batch has been finished). */
+void stop_finishers(wfe_server* s)
+{
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->finishers_stop = true;
+        s->cv_finish.notify_all();
+    }
+    for (auto& t : s->finishers)
+        if (t.joinable()) t.join();
+    s->finishers.clear();
 }
 
 void free_server(wfe_server* s)
@@ -543,8 +586,11 @@ int wfe_server_create(const wfe_server_config* cfg, wfe_server** out)
     s->stats.lanes = c.lanes;
     s->stats.memory_bytes = c.memory_bytes;
     try {
+        const uint32_t nf = std::min<uint32_t>(c.lanes, 4u);
+        for (uint32_t i = 0; i < nf; ++i) s->finishers.emplace_back(run_finisher, s);
         s->scheduler = std::thread(run_scheduler, s);
     } catch (...) {
+        stop_finishers(s);
         free_server(s);
         return WFE_ERR_INTERNAL;
     }
@@ -561,6 +607,7 @@ void wfe_server_destroy(wfe_server* s)
         s->cv_work.notify_one();
     }
     if (s->scheduler.joinable()) s->scheduler.join();
+    stop_finishers(s);
     cudaSetDevice(s->cfg.device);
     free_server(s);
 }

@@ -391,12 +391,14 @@ typedef struct wfe_server_stats {
     uint64_t peak_memory;     /* most arena bytes held at once */
     uint64_t admit_ns;        /* host time the scheduler spent forming batches and
                                  enqueueing their copies and kernels */
-    uint64_t finish_ns;       /* host time it spent copying results out and
-                                 finishing requests */
+    uint64_t finish_ns;       /* host time the finisher threads spent copying
+                                 results out and finishing requests (summed
+                                 over the threads) */
 } wfe_server_stats;
 
 /* Create a server (one context per lane, created with WFE_FLAG_DEVICE_ONLY,
- * the arena, and the scheduler thread).  WFE_ERR_BUSY when the device has
+ * the arena, the scheduler thread and up to four finisher threads that copy
+ * finished batches' results into the callers' buffers).  WFE_ERR_BUSY when the device has
  * less free memory than the arena asks for. */
 int wfe_server_create(const wfe_server_config* cfg, wfe_server** out);
 
