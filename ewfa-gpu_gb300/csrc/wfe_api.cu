@@ -53,6 +53,7 @@ struct Stage {
     uint32_t* d_lists = nullptr;  /* a work list of batch_size entries per bucket and tier */
     uint32_t* d_counts = nullptr; /* per bucket: list counts, finished CTAs, work counters */
     uint16_t* d_pred = nullptr;   /* predicted prefix distances */
+    int32_t* d_bound = nullptr;   /* distance bounds of the pairs of the CTA-per-pair tiers */
     char* h_stage = nullptr;      /* pinned gather buffer for scattered inputs */
     wfe_pair* h_pairs = nullptr;  /* pinned descriptors of a gathered batch */
     /* Scratch of tiers 2-6 owned by this stage (stage 1 only; stage 0 uses
@@ -94,6 +95,8 @@ struct BucketPlan {
     int first_tier = 0;
     int last_tier = 0;
     TierShape shape[kNumTiers] = {};
+    LongClasses cls{};      /* tier 5's distance classes (n == 0: none) */
+    TierShape bound{};      /* the bound pass (grid 0: none) */
 };
 
 struct wfe_ctx {
@@ -103,6 +106,7 @@ struct wfe_ctx {
     int nbuckets = 1;
     BucketPlan bucket[kMaxBuckets];
     bool predict = false;                      /* route pairs by predicted distance */
+    bool bound = true;                         /* bound distances before chains that start at tier 5-6 */
     int scratch_ctas[kNumTiers] = {};          /* CTAs whose global scratch is allocated */
     unsigned char* d_arena = nullptr;          /* the one allocation holding the buffers below, both
                                                   stages' work lists, counters and predictions and,
@@ -190,7 +194,9 @@ int default_first_tier(uint32_t max_len)
 /* per-stage counters, per bucket: the count of every tier's list, finished
  * CTAs and work counters of every tier; per-stage lists: one per bucket and
  * tier */
-constexpr size_t kChainWords = 3 * kNumTiers + 1;
+/* per bucket: list counts (one more for the last tier's hand-on), finished
+ * CTAs and work counters of every tier, then of every class of tier 5 */
+constexpr size_t kChainWords = 3 * kNumTiers + 1 + 3 * kLongClasses;
 constexpr size_t kCountWords = kMaxBuckets * kChainWords;
 
 /* What a stage owns itself: its staging and scratch allocations, pinned
@@ -219,6 +225,17 @@ void plan_bucket(wfe_ctx* ctx, BucketPlan& b)
             sh.scratch = ctx->d_long_scratch[t];
         }
         b.shape[t] = sh;
+    }
+    /* The bound pass and tier 5's classes, for a bucket whose pairs can reach
+     * tier 5 (a distance is at most the longer sequence's length). */
+    b.cls = LongClasses{};
+    b.bound = TierShape{};
+    if ((b.first_tier >= 5 || b.max_len > (uint32_t)tier_info(4).dcap) && b.shape[5].grid > 0) {
+        b.bound = bound_shape(b.max_len, ctx->sm_count);
+        if (b.bound.grid > 0 && ctx->d_long_scratch[5]) {
+            b.cls = long_classes(b.max_len, ctx->sm_count, ctx->long_slab[5] * (uint64_t)ctx->scratch_ctas[5]);
+            for (int k = 0; k < b.cls.n; ++k) b.cls.shape[k].scratch = ctx->d_long_scratch[5];
+        }
     }
 }
 
@@ -269,7 +286,7 @@ int launch_bucket(wfe_ctx* ctx, Stage& st, const BucketPlan& bp, int bucket_inde
     const uint32_t B = c.batch_size;
     const int t = first_tier;
     uint32_t* words = st.d_counts + (size_t)bucket_index * kChainWords;
-    uint32_t* lists = st.d_lists + (size_t)bucket_index * kNumTiers * B;
+    uint32_t* lists = st.d_lists + (size_t)bucket_index * kListsPerBucket * B;
     AlignLaunch a{};
     a.L = L;
     a.work = listed ? lists + (size_t)t * B : nullptr;
@@ -300,6 +317,25 @@ int launch_bucket(wfe_ctx* ctx, Stage& st, const BucketPlan& bp, int bucket_inde
     a.retry = t < last ? a.chain.list[t + 1] : nullptr;
     a.retry_count = words + t + 1;
     a.passed_total = ctx->d_passed + t;
+    a.cls = -1;
+    /* Distance bounds (and with them tier 5's classes) for every chain that
+     * can reach the CTA-per-pair tiers: pairs that enter tier 5 -- first or
+     * handed on -- go through the bound pass, which routes them into the
+     * classes. */
+    const bool bounded = ctx->bound && st.d_bound && bp.bound.grid > 0 && last >= 5;
+    if (bounded) {
+        a.bound = st.d_bound;
+        a.chain.bound_shape = bp.bound;
+        a.chain.cls = bp.cls;
+        uint32_t* cw = words + 3 * kNumTiers + 1;
+        for (int k = 0; k < a.chain.cls.n; ++k) {
+            a.chain.cls.list[k] = lists + (size_t)(kNumTiers + k) * B;
+            if (st.own_long_scratch[5]) a.chain.cls.shape[k].scratch = st.own_long_scratch[5];
+        }
+        a.chain.cls.counts = cw;
+        a.chain.cls.cta_done = cw + kLongClasses;
+        a.chain.cls.work_next = cw + 2 * kLongClasses;
+    }
     int grid = bp.shape[t].grid;
     if (!listed) {
         const uint32_t per_cta = t >= 5 ? 1u : 4u * (32u / (uint32_t)tier_info(t).G);
@@ -309,7 +345,17 @@ int launch_bucket(wfe_ctx* ctx, Stage& st, const BucketPlan& bp, int bucket_inde
     int rc = WFE_OK;
     TimedLaunch* tl = begin_timing(ctx, t, s, &rc);
     if (rc != WFE_OK) return rc;
-    WFE_CUDA(ctx, launch_tier(t, a, grid, s));
+    if (bounded && t == 5 && a.chain.cls.n > 0) {
+        /* tier 5 starts with the bound pass, which starts the classes */
+        WFE_CUDA(ctx, launch_bound(a, s));
+    } else {
+        if (bounded && t == 6) {
+            /* bounds only, then tier 6 */
+            WFE_CUDA(ctx, launch_bound(a, s));
+            ctx->stats.kernel_launches++;
+        }
+        WFE_CUDA(ctx, launch_tier(t, a, grid, s));
+    }
     if (tl) WFE_CUDA(ctx, cudaEventRecord(tl->stop, s));
     ctx->stats.kernel_launches++;
     ctx->stats.tier_launches[t]++;
@@ -462,13 +508,14 @@ int create_context(const wfe_config* cfg, uint64_t budget5, uint64_t budget6, wf
     const size_t nctr = 2 * kNumTiers + kMaxBuckets;
     const size_t passed_at = arena.take(sizeof(unsigned long long) * nctr);
     const size_t B = c.batch_size;
-    size_t lists_at[kStages], counts_at[kStages], pred_at[kStages];
+    size_t lists_at[kStages], counts_at[kStages], pred_at[kStages], bound_at[kStages];
     for (int i = 0; i < kStages; ++i) {
         /* a work list per tier of one length bucket; wfe_set_policy adds
          * room for more buckets */
-        lists_at[i] = arena.take((size_t)kNumTiers * B * sizeof(uint32_t));
+        lists_at[i] = arena.take((size_t)kListsPerBucket * B * sizeof(uint32_t));
         counts_at[i] = arena.take(sizeof(uint32_t) * kCountWords);
         pred_at[i] = arena.take(B * sizeof(uint16_t));
+        bound_at[i] = arena.take(B * sizeof(int32_t));
     }
     /* Host calls of several batches keep two in flight, and the second
      * stage then needs its own tier scratch: reserve it now, in the same
@@ -496,6 +543,7 @@ int create_context(const wfe_config* cfg, uint64_t budget5, uint64_t budget6, wf
         s.d_lists = reinterpret_cast<uint32_t*>(A0 + lists_at[i]);
         s.d_counts = reinterpret_cast<uint32_t*>(A0 + counts_at[i]);
         s.d_pred = reinterpret_cast<uint16_t*>(A0 + pred_at[i]);
+        s.d_bound = reinterpret_cast<int32_t*>(A0 + bound_at[i]);
     }
     if (host_pipeline) {
         Stage& s1 = ctx->st[1];
@@ -563,7 +611,7 @@ int wfe_set_policy(wfe_ctx* ctx, uint32_t nbuckets, const uint32_t* bucket_max_l
                    uint32_t flags)
 {
     if (!ctx || nbuckets < 1 || nbuckets > (uint32_t)kMaxBuckets || !bucket_max_len) return WFE_ERR_INVALID_ARGUMENT;
-    if (flags & ~(uint32_t)WFE_POLICY_PREDICT) return WFE_ERR_INVALID_ARGUMENT;
+    if (flags & ~(uint32_t)(WFE_POLICY_PREDICT | WFE_POLICY_NO_BOUND)) return WFE_ERR_INVALID_ARGUMENT;
     BucketPlan plan[kMaxBuckets];
     for (uint32_t b = 0; b < nbuckets; ++b) {
         uint32_t m = bucket_max_len[b];
@@ -581,7 +629,7 @@ int wfe_set_policy(wfe_ctx* ctx, uint32_t nbuckets, const uint32_t* bucket_max_l
     for (auto& s : ctx->st) WFE_CUDA(ctx, cudaStreamSynchronize(s.stream));
     if ((int)nbuckets > ctx->lists_buckets) {
         /* work lists for every tier of every bucket, both stages */
-        const size_t per_stage = (size_t)nbuckets * kNumTiers * ctx->cfg.batch_size;
+        const size_t per_stage = (size_t)nbuckets * kListsPerBucket * ctx->cfg.batch_size;
         uint32_t* lists = nullptr;
         WFE_CUDA(ctx, cudaMalloc(&lists, kStages * per_stage * sizeof(uint32_t)));
         cudaFree(ctx->d_lists_ext);
@@ -592,6 +640,7 @@ int wfe_set_policy(wfe_ctx* ctx, uint32_t nbuckets, const uint32_t* bucket_max_l
     ctx->nbuckets = (int)nbuckets;
     for (uint32_t b = 0; b < nbuckets; ++b) ctx->bucket[b] = plan[b];
     ctx->predict = (flags & WFE_POLICY_PREDICT) != 0;
+    ctx->bound = (flags & WFE_POLICY_NO_BOUND) == 0;
     return WFE_OK;
 }
 
@@ -600,7 +649,7 @@ int wfe_get_policy(const wfe_ctx* ctx, uint32_t* nbuckets, uint32_t* bucket_max_
 {
     if (!ctx || !nbuckets) return WFE_ERR_INVALID_ARGUMENT;
     *nbuckets = (uint32_t)ctx->nbuckets;
-    if (flags) *flags = ctx->predict ? WFE_POLICY_PREDICT : 0u;
+    if (flags) *flags = (ctx->predict ? WFE_POLICY_PREDICT : 0u) | (ctx->bound ? 0u : WFE_POLICY_NO_BOUND);
     for (int b = 0; b < ctx->nbuckets; ++b) {
         if (bucket_max_len) bucket_max_len[b] = ctx->bucket[b].max_len;
         if (first_tier) first_tier[b] = ctx->bucket[b].first_tier;

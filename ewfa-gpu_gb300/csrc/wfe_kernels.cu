@@ -25,6 +25,7 @@
 #include "wfe_kernels.cuh"
 
 #include <algorithm>
+#include <climits>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -178,8 +179,9 @@ __global__ void tier_kernel(const __grid_constant__ AlignLaunch A, uint32_t seq_
 using T0 = Tier<4, WFE_T0_J, true, 5, WFE_T0_MINB>; /* distance <= 4*J + 1 (21) */
 
 /* launched from the device too: no launch bounds (see tier_kernel) */
-template <bool GLOBAL_WF>
+template <bool GLOBAL_WF, int NT>
 __global__ void long_kernel(const __grid_constant__ AlignLaunch A);
+__global__ void bound_kernel(const __grid_constant__ AlignLaunch A, uint32_t seq_words, uint32_t unused);
 using T1 = Tier<32, 2, true, 1>;   /* distance <= 79  */
 using T2 = Tier<32, 4, false, 1>;  /* distance <= 143; backtrace store in global scratch: 8 CTAs per SM */
 using T3 = Tier<32, 8, false, 1>;  /* distance <= 271 */
@@ -218,6 +220,7 @@ __device__ __forceinline__ void tail_launch(K kernel, const AlignLaunch& A, int 
     for (unsigned i = 0; i < sizeof(AlignLaunch) / 8; ++i) dst[i] = src[i];
     AlignLaunch* n = static_cast<AlignLaunch*>(buf);
     n->tier = u;
+    n->cls = -1;
     n->work = A.chain.list[u];
     n->work_count = A.chain.counts + u;
     n->retry = u < A.chain.last_tier ? A.chain.list[u + 1] : nullptr;
@@ -245,8 +248,45 @@ __device__ __forceinline__ void launch_on_device(const AlignLaunch& A, int u, ui
     tail_launch(tier_kernel<T>, A, u, grid, kThreads, sh.smem, true, sh.seq_words, sh.gbytes);
 }
 
+/* Tail launch of distance class c of tier 5 over its list of `count`
+ * pairs.  A pair that a class hands on (its bound was not one) goes to the
+ * next class; the last class hands on to tier 6. */
+__device__ void launch_class_on_device(const AlignLaunch& A, int c, uint32_t count)
+{
+    const LongClasses& C = A.chain.cls;
+    const TierShape& sh = C.shape[c];
+    const int grid = max(1, min(sh.grid, (int)count));
+    const void* kernel = sh.threads == kLongSmallThreads ? (const void*)long_kernel<false, kLongSmallThreads>
+                                                         : (const void*)long_kernel<false, kLongThreads>;
+    void* buf = cudaGetParameterBufferV2((void*)kernel, dim3((unsigned)grid), dim3((unsigned)sh.threads), sh.smem);
+    if (!buf) {
+        note_launch_error(A, 5);
+        return;
+    }
+    const unsigned long long* src = reinterpret_cast<const unsigned long long*>(&A);
+    unsigned long long* dst = static_cast<unsigned long long*>(buf);
+#pragma unroll 4
+    for (unsigned i = 0; i < sizeof(AlignLaunch) / 8; ++i) dst[i] = src[i];
+    AlignLaunch* n = static_cast<AlignLaunch*>(buf);
+    const bool last = c + 1 >= C.n;
+    n->tier = 5;
+    n->cls = c;
+    n->work = C.list[c];
+    n->work_count = C.counts + c;
+    n->retry = !last ? C.list[c + 1] : (5 < A.chain.last_tier ? A.chain.list[6] : nullptr);
+    n->retry_count = !last ? C.counts + c + 1 : A.chain.counts + 6;
+    n->passed_total = last && A.chain.passed ? A.chain.passed + 5 : nullptr;
+    if (cudaLaunchDeviceV2(buf, cudaStreamTailLaunch) != cudaSuccess) {
+        note_launch_error(A, 5);
+        return;
+    }
+    if (A.chain.launched) atomicAdd(A.chain.launched + 5, 1ull);
+}
+
 /* Called by the last CTA of tier A.tier: tier u (> A.tier) runs over its
- * list of `count` pairs once this grid has completed. */
+ * list of `count` pairs once this grid has completed.  Tier 5 with
+ * distance classes starts with the bound pass, which routes its list into
+ * the classes. */
 __device__ void launch_tier_on_device(const AlignLaunch& A, int u, uint32_t count)
 {
     switch (u) {
@@ -255,37 +295,63 @@ __device__ void launch_tier_on_device(const AlignLaunch& A, int u, uint32_t coun
     case 3: launch_on_device<T3>(A, u, count); break;
     case 4: launch_on_device<T4>(A, u, count); break;
     case 5:
+        if (A.bound && A.chain.cls.n > 0) {
+            const TierShape& b = A.chain.bound_shape;
+            const uint32_t per_cta = (uint32_t)b.threads / 32u;
+            const int grid = max(1, min(b.grid, (int)((count + per_cta - 1u) / per_cta)));
+            tail_launch(bound_kernel, A, u, grid, b.threads, b.smem, true, b.seq_words, 0u);
+        } else {
+            const TierShape& sh = A.chain.shape[u];
+            tail_launch(long_kernel<false, kLongThreads>, A, u, max(1, min(sh.grid, (int)count)), kLongThreads,
+                        sh.smem, false, 0u, 0u);
+        }
+        break;
     case 6: {
         const TierShape& sh = A.chain.shape[u];
-        const int grid = max(1, min(sh.grid, (int)count));
-        if (u == 5)
-            tail_launch(long_kernel<false>, A, u, grid, kLongThreads, sh.smem, false, 0u, 0u);
-        else
-            tail_launch(long_kernel<true>, A, u, grid, kLongThreads, sh.smem, false, 0u, 0u);
+        tail_launch(long_kernel<true, kLongThreads>, A, u, max(1, min(sh.grid, (int)count)), kLongThreads, sh.smem,
+                    false, 0u, 0u);
         break;
     }
     default: return;
     }
 }
 
-/* End of a tier kernel: the last CTA to finish starts the next tier that has
- * work (pairs handed on by this tier, or routed to it up front). */
+/* The launch that follows this one in the chain: within tier 5 with
+ * classes (the bound pass, A.cls == -1, or class A.cls), the next class
+ * that has work; else the next tier that has work (pairs handed on, or
+ * routed to it up front). */
+__device__ void launch_next(const AlignLaunch& A)
+{
+    if (A.tier == 5 && A.chain.cls.n > 0) {
+        for (int c = A.cls + 1; c < A.chain.cls.n; ++c) {
+            const uint32_t cnt = *reinterpret_cast<volatile const uint32_t*>(A.chain.cls.counts + c);
+            if (cnt > 0u) {
+                launch_class_on_device(A, c, cnt);
+                return;
+            }
+        }
+    }
+    for (int u = A.tier + 1; u <= A.chain.last_tier; ++u) {
+        const uint32_t cnt = *reinterpret_cast<volatile const uint32_t*>(A.chain.counts + u);
+        if (cnt > 0u) {
+            launch_tier_on_device(A, u, cnt);
+            return;
+        }
+    }
+}
+
+/* End of a chained kernel: the last CTA to finish starts the next launch. */
 __device__ __forceinline__ void chain_next(const AlignLaunch& A)
 {
     if (!A.chain.cta_done) return;
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
-        const unsigned t = atomicAdd(A.chain.cta_done + A.tier, 1u);
+        uint32_t* done = A.cls >= 0 ? A.chain.cls.cta_done + A.cls : A.chain.cta_done + A.tier;
+        const unsigned t = atomicAdd(done, 1u);
         if (t == gridDim.x - 1u) {
             __threadfence();
-            for (int u = A.tier + 1; u <= A.chain.last_tier; ++u) {
-                const uint32_t cnt = *reinterpret_cast<volatile const uint32_t*>(A.chain.counts + u);
-                if (cnt > 0u) {
-                    launch_tier_on_device(A, u, cnt);
-                    break;
-                }
-            }
+            launch_next(A);
         }
     }
 }
@@ -522,13 +588,14 @@ __global__ void tier_kernel(const __grid_constant__ AlignLaunch A, uint32_t seq_
 }
 
 /* ------------------------------------------------------------------------ */
-/* Tiers 5 and 6: one CTA of 256 threads per pair, for distances beyond the
- * register tiers.  Step d computes the 2d+1 cells of [-d, d] in 32-cell
- * chunks, one warp per chunk (src/kernels.cu:111-180 with every thread of
- * the CTA); a barrier separates the steps and every thread then tests the
- * target cell (src/kernels.cu:268).  The wavefront's two buffers live in
- * shared memory (tier 5, distances up to kLongSmemDistance) or in the CTA's
- * global scratch (tier 6).  Each step also writes -1 two cells beyond its
+/* Tiers 5 and 6: one CTA of NT threads (128 or 256) per pair, for distances
+ * beyond the register tiers.  Step d computes the 2d+1 cells of [-d, d] in
+ * 32-cell chunks, one warp per chunk (src/kernels.cu:111-180 with every
+ * thread of the CTA); a barrier separates the steps and every thread then
+ * tests the target cell (src/kernels.cu:268).  The wavefront's two buffers
+ * live in shared memory (tier 5, distances up to kLongSmemDistance, or up
+ * to the limit of the launch's distance class) or in the CTA's global
+ * scratch (tier 6).  Each step also writes -1 two cells beyond its
  * range, so the next step reads the reference's sentinel there.  The 2-bit
  * backtrace store is in global scratch, row d holding ceil((2d+1)/32) 64-bit
  * entries (low and high operation bits of 32 diagonals). */
@@ -542,12 +609,14 @@ __host__ __device__ __forceinline__ uint64_t long_row(int d)
     return n + 8u * a * (a >= 1 ? a - 1 : 0) + a * (b + 1);
 }
 
-template <bool GLOBAL_WF>
+template <bool GLOBAL_WF, int NT>
 __global__ void long_kernel(const __grid_constant__ AlignLaunch A)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    constexpr int kW = kLongThreads / 32;
-    const TierShape& sh = A.chain.shape[A.tier];
+    constexpr int kW = NT / 32;
+    static_assert(kW >= 2, "warps 0 and 1 load the two sequences");
+    const bool in_class = A.cls >= 0;
+    const TierShape& sh = in_class ? A.chain.cls.shape[A.cls] : A.chain.shape[A.tier];
     const int dlim = sh.dlim;
     const int W = 2 * dlim + 5; /* entries per wavefront buffer, centre dlim + 2 */
     const int lane = (int)(threadIdx.x & 31u), warp = (int)(threadIdx.x >> 5);
@@ -569,7 +638,8 @@ __global__ void long_kernel(const __grid_constant__ AlignLaunch A)
 
     const uint32_t count = A.work_count ? min(*A.work_count, A.n_work) : A.n_work;
     __shared__ uint32_t s_item;
-    uint32_t* const work_next = A.chain.work_next ? A.chain.work_next + A.tier : nullptr;
+    uint32_t* const work_next = !A.chain.work_next ? nullptr
+                                : in_class ? A.chain.cls.work_next + A.cls : A.chain.work_next + A.tier;
     uint32_t item = blockIdx.x;
     if (work_next) {
         if (threadIdx.x == 0) s_item = atomicAdd(work_next, 1u);
@@ -587,7 +657,28 @@ __global__ void long_kernel(const __grid_constant__ AlignLaunch A)
         if (warp == 1) load_packed<32, 4>(pr.t, (uint32_t)tlen, QT, lane, kFull);
         __syncthreads();
         int D = 0;
-        if (state == ST_RUN) {
+        /* last step: the tier's limit or the caller's cap */
+        const int dstop = A.max_distance > 0 ? min(dlim, A.max_distance) : dlim;
+        /* Cone of the target.  Cell (d, kt) depends only on the cells
+         * (s, k) with |k - kt| <= d - s, so the cells that any step up to
+         * dub depends on are those with |k - kt| <= dub - s: a step computes
+         * [-d, d] cut to [kt - (dub - d), kt + (dub - d)], and every cell
+         * it reads lies in the previous step's cut range or on the -1
+         * sentinels just beyond [-(d-1), d-1].  Each cell computed holds the
+         * full recurrence's value, so the first hit at a step <= dub, and
+         * the walk back from it (which stays in the cone), are exactly the
+         * full recurrence's.  dub is dstop, or the pair's bound when one was
+         * computed below it; a pair with no hit by a bound below dstop (the
+         * bound was not one) is aligned again with dub = dstop. */
+        int dub = dstop;
+        if (state == ST_RUN && A.bound) {
+            const int bnd = A.bound[pi];
+            if (bnd >= 0 && bnd < dstop)
+                dub = max(bnd, abs(kt));
+            else if (bnd > dstop && A.retry && (A.max_distance <= 0 || A.max_distance > dlim))
+                state = ST_OVERFLOW; /* past this tier: straight to the next */
+        }
+        while (state == ST_RUN) {
             /* score 0 (src/kernels.cu:249-258) */
             if (threadIdx.x == 0) {
                 bufA[0] = extend_lane(QP, QT, plen, tlen, 0, 0);
@@ -596,21 +687,25 @@ __global__ void long_kernel(const __grid_constant__ AlignLaunch A)
             __syncthreads();
             int* prev = bufA;
             int* next = bufB;
+            bool again = false;
             if (!(kt == 0 && prev[0] == tlen)) {
                 uint2* row = ops; /* row d of the backtrace store: long_row(d), kept running */
-                /* last step: the tier's limit or the caller's cap */
-                const int dstop = A.max_distance > 0 ? min(dlim, A.max_distance) : dlim;
                 for (int d = 1;; ++d) {
-                    if (d > dstop) {
-                        state = (A.max_distance > 0 && d > A.max_distance) ? ST_OVERMAX : ST_OVERFLOW;
+                    if (d > dub) {
+                        if (dub < dstop)
+                            again = true;
+                        else
+                            state = (A.max_distance > 0 && d > A.max_distance) ? ST_OVERMAX : ST_OVERFLOW;
                         break;
                     }
                     const int ncell = 2 * d + 1;
                     const int nchunk = (ncell + 31) >> 5;
-                    for (int q = warp; q < nchunk; q += kW) {
+                    /* cells i = k + d of [ilo, ihi] */
+                    const int ilo = max(0, kt - dub + 2 * d), ihi = min(2 * d, kt + dub);
+                    for (int q = (ilo >> 5) + warp; q <= (ihi >> 5); q += kW) {
                         const int i = 32 * q + lane;
                         const int k = i - d;
-                        const bool valid = i < ncell;
+                        const bool valid = i >= ilo && i <= ihi;
                         int m = 0;
                         if (valid) {
                             m = piggyback_max(prev[k + 1], prev[k], prev[k - 1]);
@@ -627,7 +722,14 @@ __global__ void long_kernel(const __grid_constant__ AlignLaunch A)
                     row += nchunk;
                 }
             }
-            if (state == ST_RUN) state = ST_DONE;
+            if (!again) {
+                if (state == ST_RUN) state = ST_DONE;
+                break;
+            }
+            /* every thread has read the last step's target cell before
+             * thread 0 rewrites the buffers */
+            __syncthreads();
+            dub = dstop;
         }
         if (state == ST_DONE && warp == 0) {
             /* backtrace, 32 rows per round: lane r fetches row s-r's entries
@@ -704,6 +806,157 @@ __global__ void long_kernel(const __grid_constant__ AlignLaunch A)
     }
 
     chain_next(A);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Distance bounds for the CTA-per-pair tiers, one warp per pair.  The warp
+ * runs the recurrence of the tiers restricted to a band of 32 diagonals
+ * (lane l: diagonal b + l) that follows the cell furthest along its
+ * antidiagonal (largest min(h, t_len) + min(v, p_len): offsets the
+ * recurrence carries past a sequence's end count that end, so that the band
+ * turns towards the target diagonal once one sequence is consumed): one
+ * score step after it is seen the band moves one
+ * diagonal towards that cell when it lies outside lanes 15-16.  Cells
+ * outside the band count as the -1 sentinel, and a cell whose offset would
+ * put its pattern position below 0 is dropped.  Every offset the band
+ * computes is reached by some path of cost d and is at most the full
+ * recurrence's offset (the three-way maximum and the extend are both
+ * monotone), so the first step at which the band's cell (d, kt) reaches the
+ * end is an upper bound on the edit distance: bound[pi] is that step, or -1
+ * if the band has not reached it after max(p_len, t_len) + 1 steps.  On the
+ * synthetic workloads the bound equals the distance for all but a handful
+ * of pairs; the long tiers then compute only the target's cone (about half
+ * of the cells), and a bound that is not one costs a second pass, never a
+ * wrong result.  Each warp keeps its pair as plain packed words (16 bases
+ * per 32-bit word, src/kernels.cu:313-394) in shared memory, followed by
+ * zero words. */
+
+/* 16-base window of plain packed words starting at base v (words w and
+ * w + 1 of v's word w) */
+__device__ __forceinline__ uint32_t window_words(const uint32_t* W, int v)
+{
+    const int w = v >> 4;
+    return __funnelshift_l(W[w + 1], W[w], (uint32_t)(v & 15) << 1);
+}
+
+/* extend_lane over plain packed words */
+__device__ __forceinline__ int extend_words(const uint32_t* P, const uint32_t* T, int plen, int tlen, int k, int off)
+{
+    int v = off - k, h = off;
+    while ((unsigned)v < (unsigned)plen && (unsigned)h < (unsigned)tlen) {
+        const uint32_t x = window_words(P, v) ^ window_words(T, h);
+        int n = __clz(x) >> 1;
+        n = min(n, min(plen - v, tlen - h));
+        v += n;
+        h += n;
+        if (n < 16) break;
+    }
+    return h;
+}
+
+/* words per sequence in the bound kernel's shared memory: the packed words
+ * and at least one zero word after them, rounded to 16 bytes */
+__host__ __device__ __forceinline__ uint32_t bound_words(uint32_t seq_words) { return (seq_words + 4u) & ~3u; }
+
+__device__ __forceinline__ void bound_body(const AlignLaunch& A, uint32_t seq_words)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    /* tier 5 with classes: route every pair to a class, then start them */
+    const bool route = A.tier == 5 && A.chain.cls.n > 0;
+    constexpr int kW = kLongThreads / 32;
+    constexpr int kHalf = 15;
+    const int lane = (int)(threadIdx.x & 31u), warp = (int)(threadIdx.x >> 5);
+    const uint32_t bw = bound_words(seq_words);
+    uint32_t* WP = reinterpret_cast<uint32_t*>(smem) + (size_t)warp * 2u * bw;
+    uint32_t* WT = WP + bw;
+    const uint32_t count = A.work_count ? min(*A.work_count, A.n_work) : A.n_work;
+    for (uint32_t item = blockIdx.x * kW + (uint32_t)warp; item < count; item += gridDim.x * kW) {
+        const uint32_t pi = A.work ? A.work[item] : item;
+        const PairRef pr = get_pair(A.L, pi);
+        const uint32_t mx = max(pr.plen, pr.tlen);
+        int bound = -1;
+        int need = INT_MAX; /* steps the pair's class must hold */
+        if (pr.in_range && mx <= A.max_len && mx <= 16u * seq_words) {
+            const int plen = (int)pr.plen, tlen = (int)pr.tlen, kt = tlen - plen;
+            /* words 0..bw-1 of each sequence: packed_word gives 0 past the end */
+            for (uint32_t w0 = 0; w0 < bw; w0 += 32u) {
+                const uint32_t wp = packed_word<32>(pr.p, pr.plen, w0, lane, kFull);
+                const uint32_t wt = packed_word<32>(pr.t, pr.tlen, w0, lane, kFull);
+                if (w0 + (uint32_t)lane < bw) {
+                    WP[w0 + lane] = wp;
+                    WT[w0 + lane] = wt;
+                }
+            }
+            __syncwarp();
+            int b = -kHalf;
+            int O = lane == kHalf ? extend_words(WP, WT, plen, tlen, 0, 0) : -1;
+            if (__ballot_sync(kFull, lane == kHalf && kt == 0 && O == tlen)) bound = 0;
+            const int limit = (int)mx + 1;
+            int delta_next = 0;
+            for (int d = 1; bound < 0 && d <= limit; ++d) {
+                /* The band's leader after step d-1 -- the cell that has
+                 * consumed the most bases of both sequences (offsets past an
+                 * end count the end) -- moves the band of step d+1: the
+                 * reduction then runs beside step d instead of before it. */
+                const int delta = delta_next;
+                const int prog = O >= 0 ? min(O, tlen) + min(O - (b + lane), plen) : INT_MIN;
+                const int best = __reduce_max_sync(kFull, prog);
+                const int lead = __ffs((int)__ballot_sync(kFull, prog == best)) - 1 - delta;
+                delta_next = (lead > kHalf + 1) - (lead < kHalf);
+                b += delta;
+                const int k = b + lane;
+                /* diagonals k+1, k, k-1 of step d-1 were on lanes s+1, s, s-1 */
+                const int s = lane + delta;
+                int up = __shfl_sync(kFull, O, (s + 1) & 31);
+                int self = __shfl_sync(kFull, O, s & 31);
+                int dn = __shfl_sync(kFull, O, (s - 1) & 31);
+                if ((unsigned)(s + 1) > 31u) up = -1;
+                if ((unsigned)s > 31u) self = -1;
+                if ((unsigned)(s - 1) > 31u) dn = -1;
+                int N = -1;
+                if (k >= -d && k <= d) {
+                    const int off = piggyback_max(up, self, dn) >> 2;
+                    if (off >= k) N = extend_words(WP, WT, plen, tlen, k, off);
+                }
+                O = N;
+                if (__ballot_sync(kFull, k == kt && N == tlen)) bound = d;
+            }
+            if (bound >= 0) need = max(bound, abs(kt));
+            if (A.max_distance > 0) need = min(need, A.max_distance);
+        }
+        if (lane == 0) {
+            A.bound[pi] = bound;
+            if (route) {
+                const LongClasses& C = A.chain.cls;
+                const int top = C.shape[C.n - 1].dlim;
+                if (bound > top && need > top && A.retry) {
+                    /* past tier 5 (with no cap below its limit): straight on */
+                    A.retry[atomicAdd(A.retry_count, 1u)] = pi;
+                    if (A.passed_total) atomicAdd(A.passed_total, 1ull);
+                } else {
+                    int c = 0;
+                    while (c + 1 < C.n && C.shape[c].dlim < need) ++c;
+                    C.list[c][atomicAdd(C.counts + c, 1u)] = pi;
+                }
+            }
+        }
+        __syncwarp();
+    }
+    if (route) chain_next(A);
+}
+
+/* The bound pass in two forms with one body, as the tier kernels: launched
+ * from the host with launch bounds for 6 resident CTAs per SM, and from the
+ * device (a chain entering tier 5) without. */
+__global__ void __launch_bounds__(kLongThreads, 6)
+bound_kernel_host(const __grid_constant__ AlignLaunch A, uint32_t seq_words, uint32_t /* unused */)
+{
+    bound_body(A, seq_words);
+}
+
+__global__ void bound_kernel(const __grid_constant__ AlignLaunch A, uint32_t seq_words, uint32_t /* unused */)
+{
+    bound_body(A, seq_words);
 }
 
 const TierInfo kTiers[kNumTiers] = {
@@ -809,13 +1062,13 @@ __global__ void __launch_bounds__(256) classify_kernel(Layout L, uint32_t n, Buc
                     while (t < top && (float)B.dcap[t] < est) ++t;
                 }
             }
-            key = b * kNumTiers + t;
+            key = b * kListsPerBucket + t;
         }
         const unsigned same = __match_any_sync(kFull, key);
         const int leader = __ffs((int)same) - 1;
         uint32_t base = 0;
         if (key >= 0 && lane == leader) {
-            const int b = key / kNumTiers, t = key % kNumTiers;
+            const int b = key / kListsPerBucket, t = key % kListsPerBucket;
             base = atomicAdd(B.counts + (size_t)b * B.count_stride + t, (uint32_t)__popc(same));
             if (B.totals) atomicAdd(B.totals + b, (unsigned long long)__popc(same));
         }
@@ -976,25 +1229,34 @@ uint64_t long_slab_bytes(int dlim, bool global_wavefront)
 
 namespace {
 
-template <bool GWF>
-TierShape long_shape_of(uint32_t max_len, int sm_count)
+/* Shape of a CTA-per-pair launch of NT threads for sequences up to max_len
+ * and distances up to dlim (global wavefront: GWF). */
+template <bool GWF, int NT>
+TierShape long_shape_for(uint32_t max_len, int dlim, int sm_count)
 {
     TierShape sh{};
-    const int dlim = GWF ? (int)max_len : (int)std::min<uint32_t>(max_len, kLongSmemDistance);
     const uint32_t sw = seq_words_for(max_len);
     const size_t smem = 16u * (size_t)sw + (GWF ? 0u : 8u * (size_t)(2 * dlim + 5));
     if (smem > 227u * 1024u) return sh;
-    if (allow_smem((const void*)long_kernel<GWF>, smem) != cudaSuccess)
+    if (allow_smem((const void*)long_kernel<GWF, NT>, smem) != cudaSuccess)
         return sh;
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, long_kernel<GWF>, kLongThreads, smem) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, long_kernel<GWF, NT>, NT, smem) != cudaSuccess)
         return sh;
     sh.grid = std::max(1, nb) * sm_count;
     sh.smem = (uint32_t)smem;
     sh.seq_words = sw;
     sh.dlim = dlim;
     sh.slab = long_slab_bytes(dlim, GWF);
+    sh.threads = NT;
     return sh;
+}
+
+template <bool GWF>
+TierShape long_shape_of(uint32_t max_len, int sm_count)
+{
+    const int dlim = GWF ? (int)max_len : (int)std::min<uint32_t>(max_len, kLongSmemDistance);
+    return long_shape_for<GWF, kLongThreads>(max_len, dlim, sm_count);
 }
 
 template <bool GWF>
@@ -1002,9 +1264,9 @@ cudaError_t launch_long(const AlignLaunch& a, int grid, cudaStream_t s)
 {
     const TierShape& sh = a.chain.shape[a.tier];
     if (!sh.scratch || sh.smem == 0) return cudaErrorInvalidValue;
-    cudaError_t e = allow_smem((const void*)long_kernel<GWF>, sh.smem);
+    cudaError_t e = allow_smem((const void*)long_kernel<GWF, kLongThreads>, sh.smem);
     if (e != cudaSuccess) return e;
-    long_kernel<GWF><<<grid, kLongThreads, sh.smem, s>>>(a);
+    long_kernel<GWF, kLongThreads><<<grid, kLongThreads, sh.smem, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -1050,6 +1312,91 @@ TierShape tier_shape(int tier, uint32_t max_len, uint32_t cigar_stride, int sm_c
 int tier_grid(int tier, uint32_t max_len, uint32_t cigar_stride, int sm_count)
 {
     return tier_shape(tier, max_len, cigar_stride, sm_count).grid;
+}
+
+/* cached per (device, max_len, SMs), as tier_shape */
+TierShape bound_shape(uint32_t max_len, int sm_count)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return TierShape{};
+    static std::mutex mu;
+    static std::map<std::tuple<int, uint32_t, int>, TierShape> known;
+    const auto key = std::make_tuple(dev, max_len, sm_count);
+    std::lock_guard<std::mutex> lock(mu);
+    const auto it = known.find(key);
+    if (it != known.end()) return it->second;
+    TierShape sh{};
+    const uint32_t sw = seq_words_for(max_len);
+    const size_t smem = (size_t)(kLongThreads / 32) * 2u * bound_words(sw) * sizeof(uint32_t);
+    int nb = 0;
+    if (smem <= 227u * 1024u && allow_smem((const void*)bound_kernel, smem) == cudaSuccess &&
+        allow_smem((const void*)bound_kernel_host, smem) == cudaSuccess &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, bound_kernel_host, kLongThreads, smem) == cudaSuccess) {
+        sh.grid = std::max(1, nb) * sm_count;
+        sh.smem = (uint32_t)smem;
+        sh.seq_words = sw;
+        sh.threads = kLongThreads;
+    }
+    cudaGetLastError();
+    known.emplace(key, sh);
+    return sh;
+}
+
+cudaError_t launch_bound(const AlignLaunch& a, cudaStream_t s)
+{
+    const TierShape& sh = a.chain.bound_shape;
+    if (sh.grid <= 0 || !a.bound || sh.seq_words != seq_words_for(a.max_len)) return cudaErrorInvalidValue;
+    cudaError_t e = allow_smem((const void*)bound_kernel_host, sh.smem);
+    if (e != cudaSuccess) return e;
+    const uint32_t per_cta = (uint32_t)sh.threads / 32u;
+    int grid = sh.grid;
+    if (!a.work_count) grid = (int)std::min<uint64_t>((uint64_t)grid, ((uint64_t)a.n_work + per_cta - 1) / per_cta);
+    bound_kernel_host<<<std::max(grid, 1), sh.threads, sh.smem, s>>>(a, sh.seq_words, 0u);
+    return cudaGetLastError();
+}
+
+namespace {
+
+LongClasses compute_long_classes(uint32_t max_len, int sm_count, uint64_t scratch_bytes)
+{
+    LongClasses C{};
+    const int top = (int)std::min<uint32_t>(max_len, kLongSmemDistance);
+    int lim[kLongClasses];
+    int n = 0;
+    for (int c = 0; c < kLongClasses - 1; ++c)
+        if (2 * kLongClassLimit[c] < top) lim[n++] = kLongClassLimit[c];
+    lim[n++] = top;
+    for (int c = 0; c < n; ++c) {
+        TierShape sh = lim[c] <= kLongSmallDistance ? long_shape_for<false, kLongSmallThreads>(max_len, lim[c], sm_count)
+                                                    : long_shape_for<false, kLongThreads>(max_len, lim[c], sm_count);
+        if (sh.grid <= 0) return LongClasses{};
+        /* the class's slabs share tier 5's scratch: one class runs at a time */
+        const uint64_t fit = sh.slab ? scratch_bytes / sh.slab : 0u;
+        if (fit == 0) return LongClasses{};
+        sh.grid = (int)std::min<uint64_t>((uint64_t)sh.grid, fit);
+        C.shape[c] = sh;
+    }
+    C.n = n;
+    return C;
+}
+
+}  // namespace
+
+/* cached per (device, max_len, SMs, scratch), as tier_shape */
+LongClasses long_classes(uint32_t max_len, int sm_count, uint64_t scratch_bytes)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return LongClasses{};
+    static std::mutex mu;
+    static std::map<std::tuple<int, uint32_t, int, uint64_t>, LongClasses> known;
+    const auto key = std::make_tuple(dev, max_len, sm_count, scratch_bytes);
+    std::lock_guard<std::mutex> lock(mu);
+    const auto it = known.find(key);
+    if (it != known.end()) return it->second;
+    const LongClasses C = compute_long_classes(max_len, sm_count, scratch_bytes);
+    cudaGetLastError();
+    known.emplace(key, C);
+    return C;
 }
 
 cudaError_t launch_tier(int tier, const AlignLaunch& a, int grid, cudaStream_t s)

@@ -38,6 +38,32 @@ struct TierShape {
     uint32_t ops_group_bytes; /* tiers 2-4: bytes of one group's backtrace store in the global scratch */
     int ops_rows;       /* tiers 2-4: score steps that store holds (a distance never exceeds the
                            longest sequence, so rows past max_len are never written) */
+    int threads;        /* tiers 5-6 and the bound pass: threads per CTA */
+};
+
+/* Distance classes of tier 5.  The bound pass (bound_kernel) sends each pair
+ * of tier 5 to the first class whose limit covers its distance bound, and
+ * every class is a launch of its own with wavefront buffers (shared memory)
+ * and backtrace slabs sized to its limit: a class of short distances keeps
+ * two to three times the pairs in flight per SM of one launch sized for
+ * distance 2047.  Limits 255, 511 and 1023, each kept only while below half
+ * of tier 5's own limit, then tier 5's own limit (min(max_len, 2047)).
+ * Classes up to distance 1024 run CTAs of 128 threads, the last one (when
+ * larger) 256: a pair of short distance has few cells per step to share. */
+constexpr int kLongClasses = 4;
+constexpr int kLongClassLimit[kLongClasses - 1] = {255, 511, 1023};
+constexpr int kLongSmallThreads = 128;
+constexpr int kLongSmallDistance = 1024; /* classes up to this limit use kLongSmallThreads */
+/* Work lists of one length bucket: one per tier, then one per class. */
+constexpr int kListsPerBucket = kNumTiers + kLongClasses;
+
+struct LongClasses {
+    int n;                           /* classes (0: tier 5 runs as one launch over its list) */
+    TierShape shape[kLongClasses];   /* grid, smem, seq_words, dlim, slab, scratch, threads */
+    uint32_t* list[kLongClasses];
+    uint32_t* counts;                /* counts[c]: pairs in list[c] */
+    uint32_t* cta_done;              /* cta_done[c]: CTAs of class c that finished */
+    uint32_t* work_next;             /* work_next[c] */
 };
 
 /* Global scratch of one CTA of tiers 5-6 for distances up to dlim: 2-bit
@@ -61,6 +87,8 @@ struct Chain {
     unsigned long long* passed;      /* passed[t]: pairs tier t handed on (stats) */
     uint8_t* launch_error;           /* byte t set: a device-side launch of tier t failed (host memory
                                         the device writes in place) */
+    LongClasses cls;                 /* tier 5's distance classes */
+    TierShape bound_shape;           /* the bound pass: grid, smem, seq_words, threads */
 };
 
 /* Length buckets of the classify kernel, and for each the tiers a pair may
@@ -74,7 +102,7 @@ struct Buckets {
     int last_tier[kMaxBuckets];
     int dcap[kNumTiers];             /* largest distance of each tier */
     const uint16_t* pred;            /* predicted prefix distances, or NULL (route to first_tier) */
-    uint32_t* lists;                 /* list of bucket b, tier t at lists + (b*kNumTiers + t)*stride */
+    uint32_t* lists;                 /* list of bucket b, tier t at lists + (b*kListsPerBucket + t)*stride */
     uint32_t stride;
     uint32_t* counts;                /* counts of bucket b at counts + b*count_stride */
     uint32_t count_stride;
@@ -98,6 +126,11 @@ struct AlignLaunch {
     uint32_t* retry_count;
     unsigned long long* passed_total; /* running count of pairs handed on (stats) */
     uint16_t* pred;              /* prediction launch: prefix distance of every pair */
+    int32_t* bound;              /* tiers 5-6: an upper bound on each pair's distance (by pair
+                                    index; -1 = none), written by the bound pass; NULL = none */
+    int cls;                     /* tier 5: the distance class of this launch; -1 = the bound pass
+                                    (which routes tier 5's list into the classes) or, without
+                                    classes, tier 5 as one launch */
     unsigned char* ops_scratch;  /* global op store for tiers that keep it there */
     size_t ops_scratch_bytes;
     int tier;                    /* this launch's tier */
@@ -116,6 +149,20 @@ size_t tier_scratch_bytes(int tier, int grid, uint32_t max_len);
  * cigar_stride (occupancy-limited, at least 1). */
 int tier_grid(int tier, uint32_t max_len, uint32_t cigar_stride, int sm_count);
 cudaError_t launch_tier(int tier, const AlignLaunch& a, int grid, cudaStream_t s);
+
+/* Upper bounds on the distances of the pairs of a CTA-per-pair tier's work
+ * list (a.work / a.work_count / a.n_work, sequences up to a.max_len) into
+ * a.bound, one warp per pair; see bound_kernel.  With a.tier == 5 and
+ * classes (a.chain.cls.n > 0) the pass also routes every pair to its class
+ * and its last CTA starts the first class that has work (tier 5 as a chain
+ * of class launches).  bound_shape: its launch shape (grid 0: its shared
+ * memory does not fit, and no bound can be computed). */
+TierShape bound_shape(uint32_t max_len, int sm_count);
+cudaError_t launch_bound(const AlignLaunch& a, cudaStream_t s);
+
+/* Tier 5's distance classes for sequences up to max_len, their slabs carved
+ * from a tier-5 scratch of scratch_bytes (0 classes: none fits). */
+LongClasses long_classes(uint32_t max_len, int sm_count, uint64_t scratch_bytes);
 
 /* Sort pairs 0..n-1 into length buckets by max(p_len, t_len) and, within a
  * bucket, into the tier of their predicted distance (see Buckets). */

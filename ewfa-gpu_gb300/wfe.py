@@ -28,6 +28,7 @@ FLAG_KERNEL_TIMING = 2
 FLAG_DEVICE_ONLY = 4
 FLAG_PAGEABLE_IN_PLACE = 8
 POLICY_PREDICT = 1
+POLICY_NO_BOUND = 2
 
 PAIR_DTYPE = np.dtype([("p_off", "<u8"), ("t_off", "<u8"), ("p_len", "<u4"), ("t_len", "<u4")])
 assert PAIR_DTYPE.itemsize == 24
@@ -326,13 +327,14 @@ class Context:
     def reset_stats(self) -> None:
         _check(load().wfe_reset_stats(self._h), "wfe_reset_stats")
 
-    def set_policy(self, bucket_max_len, first_tier=None, predict: bool = False) -> None:
+    def set_policy(self, bucket_max_len, first_tier=None, predict: bool = False, bound: bool = True) -> None:
         """Length buckets (ascending max lengths), each bucket's first tier
-        (-1 = by length) and distance prediction; see wfe_set_policy."""
+        (-1 = by length), distance prediction and the distance bounds of the
+        CTA-per-pair tiers; see wfe_set_policy."""
         bm = np.ascontiguousarray(bucket_max_len, dtype=np.uint32)
         ft = None if first_tier is None else np.ascontiguousarray(first_tier, dtype=np.int32)
-        _check(load().wfe_set_policy(self._h, len(bm), _addr(bm), _addr(ft), POLICY_PREDICT if predict else 0),
-               "wfe_set_policy")
+        flags = (POLICY_PREDICT if predict else 0) | (0 if bound else POLICY_NO_BOUND)
+        _check(load().wfe_set_policy(self._h, len(bm), _addr(bm), _addr(ft), flags), "wfe_set_policy")
 
     def policy(self):
         nb, fl = C.c_uint32(0), C.c_uint32(0)

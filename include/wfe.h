@@ -188,9 +188,16 @@ int wfe_reset_stats(wfe_ctx* ctx);
  * length: pairs of one length but very different error rates no longer all
  * start at the same tier (and restart in every tier they outgrow).  Results
  * do not depend on the policy.  The default is one bucket, no prediction.
+ * A chain that starts at tier 5 or 6 first bounds the distance of each of its
+ * pairs with a narrow band of the wavefront (one warp per pair); the
+ * CTA-per-pair tiers then compute only the cells the target cell depends on
+ * (about half of them), and a pair whose bound lies past tier 5's limit
+ * goes straight to tier 6.  WFE_POLICY_NO_BOUND turns that pass off (for
+ * comparison: results are the same).
  * Replaces nothing in the reference, which has one fixed launch shape
  * (src/wavefront.cu:173-208); see also wfe_autotune. */
-#define WFE_POLICY_PREDICT 1u /* route every pair to the tier of its predicted distance */
+#define WFE_POLICY_PREDICT 1u  /* route every pair to the tier of its predicted distance */
+#define WFE_POLICY_NO_BOUND 2u /* no distance bounds before the CTA-per-pair tiers */
 int wfe_set_policy(wfe_ctx* ctx, uint32_t nbuckets, const uint32_t* bucket_max_len,
                    const int32_t* first_tier, uint32_t flags);
 int wfe_get_policy(const wfe_ctx* ctx, uint32_t* nbuckets, uint32_t* bucket_max_len,

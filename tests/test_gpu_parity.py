@@ -602,6 +602,41 @@ def test_long_tiers_in_one_slab_each():
     assert_same_cigars(got[1], want[1])
 
 
+def test_distance_classes_and_bounds():
+    """Tier 5 first: the bound pass routes the pairs into the distance classes
+    (limits 255, 511, 1023 and 2047 for 5,000-base sequences) and straight
+    to tier 6 past 2047; short and long distances, near-identical and
+    unrelated pairs, unequal lengths.  The same results with the bound pass
+    off (one launch of tier 5 over every pair), and the oracle's."""
+    torch_cuda()
+    rng = np.random.default_rng(77)
+    ascii, pairs = wfe.generate(600, 200, 4800, p_min=0.0, p_max=0.3, seed=77)
+    seqs = [(ascii[q["p_off"]:q["p_off"] + q["p_len"]].tobytes(), ascii[q["t_off"]:q["t_off"] + q["t_len"]].tobytes())
+            for q in pairs]
+    a2, p2 = _long_tier_pairs()
+    seqs += [(a2[q["p_off"]:q["p_off"] + q["p_len"]].tobytes(), a2[q["t_off"]:q["t_off"] + q["t_len"]].tobytes())
+             for q in p2]
+    t = np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, 3000)].tobytes()
+    seqs += [(t, t), (t[:1000], t), (t, t[:2200]), (b"", t[:300]), (b"A", b"")]
+    ascii, pairs = wfe.pairs_from_list(seqs)
+    got = {}
+    for bound in (True, False):
+        with wfe.Context(max_seq_len=5000, cigar_stride=12000, batch_size=400) as ctx:
+            ctx.set_policy([5000], [5], bound=bound)
+            got[bound] = ctx.align(ascii, pairs)
+            stats = ctx.stats()
+        assert stats["tier_passed"][5] > 0, stats
+        if bound:
+            # the bound pass and more than one class per batch
+            assert stats["tier_launches"][5] > 2 * stats["batches"], stats
+    dist, cg, st = got[True]
+    assert (st == 0).all() and dist.max() > 2047 and (dist < 255).sum() > 50
+    np.testing.assert_array_equal(dist, got[False][0])
+    np.testing.assert_array_equal(st, got[False][2])
+    assert_same_cigars(cg, got[False][1])
+    compare_with_oracle(ascii, pairs, 12000, dist, cg, st)
+
+
 @pytest.mark.parametrize("first_tier", [5, 6])
 def test_cta_tiers_first_with_and_without_cap(first_tier):
     """The CTA-per-pair tiers as the first tier of every pair: identical
