@@ -195,8 +195,9 @@ int default_first_tier(uint32_t max_len)
  * CTAs and work counters of every tier; per-stage lists: one per bucket and
  * tier */
 /* per bucket: list counts (one more for the last tier's hand-on), finished
- * CTAs and work counters of every tier, then of every class of tier 5 */
-constexpr size_t kChainWords = 3 * kNumTiers + 1 + 3 * kLongClasses;
+ * CTAs and work counters of every tier, then, for every class of tier 5,
+ * front and back list counts, finished CTAs and work counters */
+constexpr size_t kChainWords = 3 * kNumTiers + 1 + 4 * kLongClasses;
 constexpr size_t kCountWords = kMaxBuckets * kChainWords;
 
 /* What a stage owns itself: its staging and scratch allocations, pinned
@@ -332,9 +333,11 @@ int launch_bucket(wfe_ctx* ctx, Stage& st, const BucketPlan& bp, int bucket_inde
             a.chain.cls.list[k] = lists + (size_t)(kNumTiers + k) * B;
             if (st.own_long_scratch[5]) a.chain.cls.shape[k].scratch = st.own_long_scratch[5];
         }
+        a.chain.cls.cap = B;
         a.chain.cls.counts = cw;
-        a.chain.cls.cta_done = cw + kLongClasses;
-        a.chain.cls.work_next = cw + 2 * kLongClasses;
+        a.chain.cls.low_counts = cw + kLongClasses;
+        a.chain.cls.cta_done = cw + 2 * kLongClasses;
+        a.chain.cls.work_next = cw + 3 * kLongClasses;
     }
     int grid = bp.shape[t].grid;
     if (!listed) {

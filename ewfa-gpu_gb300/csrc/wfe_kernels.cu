@@ -324,7 +324,8 @@ __device__ void launch_next(const AlignLaunch& A)
 {
     if (A.tier == 5 && A.chain.cls.n > 0) {
         for (int c = A.cls + 1; c < A.chain.cls.n; ++c) {
-            const uint32_t cnt = *reinterpret_cast<volatile const uint32_t*>(A.chain.cls.counts + c);
+            const uint32_t cnt = *reinterpret_cast<volatile const uint32_t*>(A.chain.cls.counts + c) +
+                                 *reinterpret_cast<volatile const uint32_t*>(A.chain.cls.low_counts + c);
             if (cnt > 0u) {
                 launch_class_on_device(A, c, cnt);
                 return;
@@ -636,7 +637,9 @@ __global__ void long_kernel(const __grid_constant__ AlignLaunch A)
     int* bufA = wf + dlim + 2;     /* centred */
     int* bufB = wf + W + dlim + 2;
 
-    const uint32_t count = A.work_count ? min(*A.work_count, A.n_work) : A.n_work;
+    /* a class list: its front part, then its back part from the end */
+    const uint32_t front = A.work_count ? *A.work_count : A.n_work;
+    const uint32_t count = min(front + (in_class ? A.chain.cls.low_counts[A.cls] : 0u), A.n_work);
     __shared__ uint32_t s_item;
     uint32_t* const work_next = !A.chain.work_next ? nullptr
                                 : in_class ? A.chain.cls.work_next + A.cls : A.chain.work_next + A.tier;
@@ -647,7 +650,7 @@ __global__ void long_kernel(const __grid_constant__ AlignLaunch A)
         item = s_item;
     }
     while (item < count) {
-        const uint32_t pi = A.work ? A.work[item] : item;
+        const uint32_t pi = !A.work ? item : item < front ? A.work[item] : A.work[A.chain.cls.cap - 1u - (item - front)];
         const PairRef pr = get_pair(A.L, pi);
         const uint32_t mx = max(pr.plen, pr.tlen);
         int state = !pr.in_range ? ST_RANGE : (mx > A.max_len || mx > 16u * seq_words) ? ST_TOOLONG : ST_RUN;
@@ -936,7 +939,11 @@ __device__ __forceinline__ void bound_body(const AlignLaunch& A, uint32_t seq_wo
                 } else {
                     int c = 0;
                     while (c + 1 < C.n && C.shape[c].dlim < need) ++c;
-                    C.list[c][atomicAdd(C.counts + c, 1u)] = pi;
+                    const int below = c > 0 ? C.shape[c - 1].dlim : 0;
+                    if (2 * need >= below + C.shape[c].dlim)
+                        C.list[c][atomicAdd(C.counts + c, 1u)] = pi;
+                    else
+                        C.list[c][C.cap - 1u - atomicAdd(C.low_counts + c, 1u)] = pi;
                 }
             }
         }

@@ -60,8 +60,14 @@ constexpr int kListsPerBucket = kNumTiers + kLongClasses;
 struct LongClasses {
     int n;                           /* classes (0: tier 5 runs as one launch over its list) */
     TierShape shape[kLongClasses];   /* grid, smem, seq_words, dlim, slab, scratch, threads */
+    /* List c holds the pairs of the upper half of the class's distances from
+     * its front (counts[c] of them) and the others from its back
+     * (low_counts[c], at cap-1, cap-2, ...): a class launch takes its longer
+     * pairs first, so that its last CTAs are not left with them. */
     uint32_t* list[kLongClasses];
-    uint32_t* counts;                /* counts[c]: pairs in list[c] */
+    uint32_t cap;                    /* entries of each list */
+    uint32_t* counts;                /* counts[c]: pairs at the front of list[c] */
+    uint32_t* low_counts;            /* low_counts[c]: pairs at its back */
     uint32_t* cta_done;              /* cta_done[c]: CTAs of class c that finished */
     uint32_t* work_next;             /* work_next[c] */
 };
