@@ -23,6 +23,7 @@
  *   - a sequence longer than 2*l is an error instead of a buffer overrun, and
  *     a last line without '\n' keeps its last base.
  */
+#include <algorithm>
 #include <cinttypes>
 #include <cstdio>
 #include <cstdlib>
@@ -105,14 +106,21 @@ double now_s()
 
 struct Share {
     size_t first = 0, n = 0;
+    size_t batch = 0;  /* batch size of its context */
+    size_t window = 0; /* pairs per wfe_align call: the results arrays hold that many */
     /* never initialised: helper threads only make the pages present, and
      * the kernels write the results in place */
     std::unique_ptr<int32_t[]> dist;
     std::unique_ptr<int8_t[]> cigar;
     std::unique_ptr<uint8_t[]> status;
+    wfe_ctx* ctx = nullptr;
     int rc = WFE_OK;
     std::string what;
 };
+
+/* Results arrays of at most this many bytes per share, written over and
+ * over by the share's wfe_align calls (a whole share when it fits). */
+constexpr size_t kWindowBytes = size_t(256) << 20;
 
 }  // namespace
 
@@ -178,64 +186,38 @@ int main(int argc, char** argv)
         return 1;
     }
 
-    /* read the file before the clock starts, like the reference */
-    wfe_pair_file pf{};
-    char err[256] = {0};
-    if (wfe_read_pair_file(path.c_str(), (size_t)n_req, (int)std::thread::hardware_concurrency(), 1, &pf, err,
-                           sizeof err) != WFE_OK) {
-        std::fprintf(stderr, "%s\n", err);
-        std::fprintf(stderr, "Could not read the sequences from file %s\n", path.c_str());
-        return 1;
-    }
-    struct Release {
-        wfe_pair_file* f;
-        ~Release() { wfe_free_pair_file(f); }
-    } release{&pf};
     const uint32_t max_len = (uint32_t)(2 * seq_len); /* the reader's slot holds 2*l bases */
-    if (pf.longest > max_len) {
-        std::fprintf(stderr, "A sequence of %u bases is longer than 2*l = %u.\n", pf.longest, max_len);
-        return 1;
-    }
-    /* pairs the file does not have are empty (utils/sequence_reader.cu:30) */
-    std::vector<wfe_pair> tail;
-    if (pf.n < (size_t)n_req) {
-        std::fprintf(stderr, "The file holds %zu pairs; the other %lld are empty.\n", pf.n,
-                     n_req - (long long)pf.n);
-        tail.assign((size_t)n_req - pf.n, wfe_pair{0, 0, 0, 0});
-    }
     const size_t N = (size_t)n_req;
-    auto pair_at = [&](size_t i) -> const wfe_pair* { return i < pf.n ? pf.pairs + i : tail.data() + (i - pf.n); };
     const uint32_t stride = (uint32_t)(seq_len + (4 - seq_len % 4)); /* cigar_max_len */
-
     const bool keep = print || check;
-    const double t0 = now_s();
+
+    /* Every share's context and results arrays are set up by a thread of
+     * its own while the main thread reads the file: the shares, batch sizes
+     * and sequence length are known from the arguments.  The results arrays
+     * are made present page by page (the first touch of a page is the slow
+     * part of the kernels writing them in place).  The timed region starts
+     * after the read, as the reference's does, and includes any part of the
+     * set-up still running then. */
     std::vector<Share> shares((size_t)threads);
-    auto worker = [&](size_t t) {
+    auto prepare = [&](size_t t) {
         Share& sh = shares[t];
-        size_t per = N / (size_t)threads;
+        const size_t per = N / (size_t)threads;
         sh.first = per * t;
         sh.n = per + (t == (size_t)threads - 1 ? N % (size_t)threads : 0);
-        size_t b = (size_t)batch;
-        if (b > sh.n) {
-            if (sh.n) std::fprintf(stderr, "[Thread %zu] Changing batch size to %zu", t, sh.n);
-            b = sh.n;
-        }
+        sh.batch = std::min((size_t)batch, sh.n);
         if (sh.n == 0) return;
-        /* Results that are printed or checked are kept for the whole share.
-         * Otherwise, as the reference keeps one batch of CIGARs on the host
-         * (src/wavefront.cu:267-300), a window of two batches (both
-         * pipeline stages busy) is written over and over.  The window's
-         * fresh pages are made present by four helper threads while the
-         * context is created: the kernels write them in place, and the first
-         * touch of a page (the kernel zeroing it) is the slow part. */
-        const size_t window = keep ? sh.n : std::min(sh.n, 2 * b);
-        sh.dist.reset(new int32_t[window]);
-        sh.cigar.reset(new int8_t[window * stride]);
-        sh.status.reset(new uint8_t[window]);
+        /* Results that are printed or checked are kept for the whole
+         * share; otherwise a window of up to kWindowBytes is written over
+         * and over (the reference keeps one batch, src/wavefront.cu:267-300). */
+        const size_t cap = std::max<size_t>(2 * sh.batch, kWindowBytes / ((size_t)stride + 5u));
+        sh.window = keep ? sh.n : std::min(sh.n, cap);
+        sh.dist.reset(new int32_t[sh.window]);
+        sh.cigar.reset(new int8_t[sh.window * stride]);
+        sh.status.reset(new uint8_t[sh.window]);
         std::vector<std::thread> touch;
         {
             char* ranges[3] = {(char*)sh.dist.get(), (char*)sh.cigar.get(), (char*)sh.status.get()};
-            const size_t bytes[3] = {window * sizeof(int32_t), window * (size_t)stride, window};
+            const size_t bytes[3] = {sh.window * sizeof(int32_t), sh.window * (size_t)stride, sh.window};
             constexpr unsigned kTouchThreads = 4;
             for (unsigned k = 0; k < kTouchThreads; ++k)
                 touch.emplace_back([=] {
@@ -250,17 +232,64 @@ int main(int argc, char** argv)
         wfe_config cfg{};
         cfg.device = device;
         cfg.max_seq_len = max_len;
-        cfg.batch_size = (uint32_t)b;
+        cfg.batch_size = (uint32_t)sh.batch;
         cfg.max_distance = (int32_t)max_distance;
         cfg.cigar_stride = stride;
         cfg.flags = WFE_FLAG_PAGEABLE_IN_PLACE; /* the results go straight to this share's arrays */
-        wfe_ctx* ctx = nullptr;
-        sh.rc = wfe_create(&cfg, &ctx);
+        sh.rc = wfe_create(&cfg, &sh.ctx);
+        if (sh.rc != WFE_OK) sh.what = "wfe_create";
         for (auto& x : touch) x.join();
-        if (sh.rc != WFE_OK) {
-            sh.what = "wfe_create";
-            return;
+    };
+    std::vector<std::thread> setup;
+    for (size_t t = 0; t < (size_t)threads; ++t) setup.emplace_back(prepare, t);
+    struct Teardown {
+        std::vector<std::thread>& setup;
+        std::vector<Share>& shares;
+        ~Teardown()
+        {
+            for (auto& x : setup)
+                if (x.joinable()) x.join();
+            for (Share& sh : shares)
+                if (sh.ctx) wfe_destroy(sh.ctx);
         }
+    } teardown{setup, shares};
+
+    /* read the file before the clock starts, like the reference */
+    wfe_pair_file pf{};
+    char err[256] = {0};
+    if (wfe_read_pair_file(path.c_str(), (size_t)n_req, (int)std::thread::hardware_concurrency(), 1, &pf, err,
+                           sizeof err) != WFE_OK) {
+        std::fprintf(stderr, "%s\n", err);
+        std::fprintf(stderr, "Could not read the sequences from file %s\n", path.c_str());
+        return 1;
+    }
+    struct Release {
+        wfe_pair_file* f;
+        ~Release() { wfe_free_pair_file(f); }
+    } release{&pf};
+    if (pf.longest > max_len) {
+        std::fprintf(stderr, "A sequence of %u bases is longer than 2*l = %u.\n", pf.longest, max_len);
+        return 1;
+    }
+    /* pairs the file does not have are empty (utils/sequence_reader.cu:30) */
+    std::vector<wfe_pair> tail;
+    if (pf.n < (size_t)n_req) {
+        std::fprintf(stderr, "The file holds %zu pairs; the other %lld are empty.\n", pf.n,
+                     n_req - (long long)pf.n);
+        tail.assign((size_t)n_req - pf.n, wfe_pair{0, 0, 0, 0});
+    }
+    auto pair_at = [&](size_t i) -> const wfe_pair* { return i < pf.n ? pf.pairs + i : tail.data() + (i - pf.n); };
+
+    const double t0 = now_s();
+    for (auto& x : setup) x.join();
+    for (size_t t = 0; t < shares.size(); ++t)
+        if (shares[t].n && shares[t].batch < (size_t)batch)
+            std::fprintf(stderr, "[Thread %zu] Changing batch size to %zu", t, shares[t].batch);
+    auto worker = [&](size_t t) {
+        Share& sh = shares[t];
+        if (sh.n == 0 || sh.rc != WFE_OK) return;
+        wfe_ctx* ctx = sh.ctx;
+        const size_t window = sh.window;
         /* the pairs of this share: in the file's pinned descriptors, or the
          * empty tail */
         std::vector<wfe_pair> mine;
@@ -276,6 +305,7 @@ int main(int argc, char** argv)
         }
         if (sh.rc != WFE_OK) sh.what = "wfe_align";
         wfe_destroy(ctx);
+        sh.ctx = nullptr;
     };
     {
         std::vector<std::thread> th;
