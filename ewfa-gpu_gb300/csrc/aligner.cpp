@@ -108,14 +108,26 @@ struct Share {
     size_t first = 0, n = 0;
     size_t batch = 0;  /* batch size of its context */
     size_t window = 0; /* pairs per wfe_align call: the results arrays hold that many */
-    /* never initialised: helper threads only make the pages present, and
-     * the kernels write the results in place */
-    std::unique_ptr<int32_t[]> dist;
-    std::unique_ptr<int8_t[]> cigar;
-    std::unique_ptr<uint8_t[]> status;
+    /* One buffer for the results arrays, page-locked when possible (the
+     * kernels then write it in place like any pinned output), else
+     * ordinary memory whose pages helper threads make present.  Never
+     * initialised: the kernels write every result. */
+    char* buf = nullptr;
+    bool pinned = false;
+    int32_t* dist = nullptr;
+    int8_t* cigar = nullptr;
+    uint8_t* status = nullptr;
     wfe_ctx* ctx = nullptr;
     int rc = WFE_OK;
     std::string what;
+    Share() = default;
+    Share(const Share&) = delete;
+    Share& operator=(const Share&) = delete;
+    ~Share()
+    {
+        if (pinned) wfe_host_free(buf);
+        else delete[] buf;
+    }
 };
 
 /* Results arrays of at most this many bytes per share, written over and
@@ -211,22 +223,28 @@ int main(int argc, char** argv)
          * and over (the reference keeps one batch, src/wavefront.cu:267-300). */
         const size_t cap = std::max<size_t>(2 * sh.batch, kWindowBytes / ((size_t)stride + 5u));
         sh.window = keep ? sh.n : std::min(sh.n, cap);
-        sh.dist.reset(new int32_t[sh.window]);
-        sh.cigar.reset(new int8_t[sh.window * stride]);
-        sh.status.reset(new uint8_t[sh.window]);
+        /* dist, then the CIGAR slots (the stride is a multiple of 4), then status */
+        const size_t total = sh.window * (sizeof(int32_t) + (size_t)stride + 1u);
+        void* pinned = nullptr;
+        if (wfe_host_alloc(&pinned, total) == WFE_OK) {
+            sh.buf = static_cast<char*>(pinned);
+            sh.pinned = true;
+        } else {
+            sh.buf = new char[total];
+        }
+        sh.dist = reinterpret_cast<int32_t*>(sh.buf);
+        sh.cigar = reinterpret_cast<int8_t*>(sh.buf + sh.window * sizeof(int32_t));
+        sh.status = reinterpret_cast<uint8_t*>(sh.buf + sh.window * (sizeof(int32_t) + (size_t)stride));
         std::vector<std::thread> touch;
-        {
-            char* ranges[3] = {(char*)sh.dist.get(), (char*)sh.cigar.get(), (char*)sh.status.get()};
-            const size_t bytes[3] = {sh.window * sizeof(int32_t), sh.window * (size_t)stride, sh.window};
+        if (!sh.pinned) {
+            char* base = sh.buf;
             constexpr unsigned kTouchThreads = 4;
             for (unsigned k = 0; k < kTouchThreads; ++k)
                 touch.emplace_back([=] {
                     const size_t page = 4096; /* every 4 KiB: covers any page size */
-                    for (int r = 0; r < 3; ++r) {
-                        const size_t lo = bytes[r] * k / kTouchThreads, hi = bytes[r] * (k + 1) / kTouchThreads;
-                        for (size_t i = lo; i < hi; i += page) ranges[r][i] = 0;
-                        if (hi > lo) ranges[r][hi - 1] = 0;
-                    }
+                    const size_t lo = total * k / kTouchThreads, hi = total * (k + 1) / kTouchThreads;
+                    for (size_t i = lo; i < hi; i += page) base[i] = 0;
+                    if (hi > lo) base[hi - 1] = 0;
                 });
         }
         wfe_config cfg{};
@@ -300,8 +318,8 @@ int main(int argc, char** argv)
             src = mine.data();
         }
         for (size_t c0 = 0; c0 < sh.n && sh.rc == WFE_OK; c0 += window) {
-            sh.rc = wfe_align(ctx, pf.ascii, pf.ascii_bytes, src + c0, std::min(window, sh.n - c0), sh.dist.get(),
-                              sh.cigar.get(), sh.status.get());
+            sh.rc = wfe_align(ctx, pf.ascii, pf.ascii_bytes, src + c0, std::min(window, sh.n - c0), sh.dist,
+                              sh.cigar, sh.status);
         }
         if (sh.rc != WFE_OK) sh.what = "wfe_align";
         wfe_destroy(ctx);
