@@ -227,11 +227,12 @@ void plan_bucket(wfe_ctx* ctx, BucketPlan& b)
         }
         b.shape[t] = sh;
     }
-    /* The bound pass and tier 5's classes, for a bucket whose pairs can reach
-     * tier 5 (a distance is at most the longer sequence's length). */
+    /* The bound pass and tier 5's classes (shapes cached per process, like
+     * the tiers'); the autotuner also tries tier 5 first on buckets whose
+     * pairs would not reach it otherwise. */
     b.cls = LongClasses{};
     b.bound = TierShape{};
-    if ((b.first_tier >= 5 || b.max_len > (uint32_t)tier_info(4).dcap) && b.shape[5].grid > 0) {
+    if (b.shape[5].grid > 0) {
         b.bound = bound_shape(b.max_len, ctx->sm_count);
         if (b.bound.grid > 0 && ctx->d_long_scratch[5]) {
             b.cls = long_classes(b.max_len, ctx->sm_count, ctx->long_slab[5] * (uint64_t)ctx->scratch_ctas[5]);
