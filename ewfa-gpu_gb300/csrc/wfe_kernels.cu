@@ -256,8 +256,9 @@ __device__ void launch_class_on_device(const AlignLaunch& A, int c, uint32_t cou
     const LongClasses& C = A.chain.cls;
     const TierShape& sh = C.shape[c];
     const int grid = max(1, min(sh.grid, (int)count));
-    const void* kernel = sh.threads == kLongSmallThreads ? (const void*)long_kernel<false, kLongSmallThreads>
-                                                         : (const void*)long_kernel<false, kLongThreads>;
+    const void* kernel = sh.threads == kLongTinyThreads    ? (const void*)long_kernel<false, kLongTinyThreads>
+                         : sh.threads == kLongSmallThreads ? (const void*)long_kernel<false, kLongSmallThreads>
+                                                           : (const void*)long_kernel<false, kLongThreads>;
     void* buf = cudaGetParameterBufferV2((void*)kernel, dim3((unsigned)grid), dim3((unsigned)sh.threads), sh.smem);
     if (!buf) {
         note_launch_error(A, 5);
@@ -1374,7 +1375,8 @@ LongClasses compute_long_classes(uint32_t max_len, int sm_count, uint64_t scratc
         if (2 * kLongClassLimit[c] < top) lim[n++] = kLongClassLimit[c];
     lim[n++] = top;
     for (int c = 0; c < n; ++c) {
-        TierShape sh = lim[c] <= kLongSmallDistance ? long_shape_for<false, kLongSmallThreads>(max_len, lim[c], sm_count)
+        TierShape sh = lim[c] <= kLongTinyDistance    ? long_shape_for<false, kLongTinyThreads>(max_len, lim[c], sm_count)
+                     : lim[c] <= kLongSmallDistance ? long_shape_for<false, kLongSmallThreads>(max_len, lim[c], sm_count)
                                                     : long_shape_for<false, kLongThreads>(max_len, lim[c], sm_count);
         if (sh.grid <= 0) return LongClasses{};
         /* the class's slabs share tier 5's scratch: one class runs at a time */
