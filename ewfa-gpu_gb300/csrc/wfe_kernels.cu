@@ -6,6 +6,12 @@
  *                        backtrace store, backtrace and CIGAR replay for one
  *                        pair per group of G lanes (src/kernels.cu:27-310 and
  *                        397-625 in one kernel)
+ *   long_kernel<GWF, NT> the same for one pair per CTA of NT threads
+ *                        (tiers 5-6), over the target's cone when the pair
+ *                        has a distance bound
+ *   bound_kernel         distance bounds from a 32-diagonal band, one warp
+ *                        per pair; routes tier 5's pairs to distance classes
+ *   classify_kernel      length buckets and predicted tiers
  *   history_cigar_kernel CIGARs from the reference's 128-bit histories
  *                        (src/kernels.cu:397-625)
  *
