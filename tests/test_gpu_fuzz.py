@@ -1,7 +1,9 @@
 """Randomised differential tests: libwfe against the CPU oracle over seeded
 random configurations -- lengths from 0 to 1,200 bases, edit probabilities up
 to 0.4, distance caps, CIGAR slots too small for some CIGARs, batch sizes,
-length buckets with and without distance prediction, and every host and
+length buckets with and without distance prediction, the CTA-per-pair tier
+as the first tier of every pair (the bound pass, the target's cone and the
+distance classes, or one launch without bounds), and every host and
 device entry point (pageable staged, pageable in place, pinned in place,
 device buffers, the reference reader's strided layout).  Integer work: every
 distance, status and CIGAR byte must match."""
@@ -31,7 +33,7 @@ def random_case(k):
         batch=int(rng.choice([37, 256, 1000, 100000])),
         stride=int(rng.choice([8, 40, wfe.reference_cigar_stride(longest), 2 * longest + 8])),
         mode=MODES[k % len(MODES)],
-        policy=str(rng.choice(["default", "buckets", "predict"])))
+        policy=str(rng.choice(["default", "buckets", "predict", "tier5", "tier5_nobound"])))
 
 
 def run_case(ascii, pairs, c):
@@ -39,7 +41,9 @@ def run_case(ascii, pairs, c):
     n, S = len(pairs), c["stride"]
     with wfe.Context(max_seq_len=c["max_len"], batch_size=c["batch"], max_distance=c["max_distance"],
                      cigar_stride=S, flags=flags) as ctx:
-        if c["policy"] != "default":
+        if c["policy"] in ("tier5", "tier5_nobound"):
+            ctx.set_policy([c["max_len"]], [5], bound=c["policy"] == "tier5")
+        elif c["policy"] != "default":
             cuts = sorted({max(1, c["max_len"] // 4), max(1, c["max_len"] // 2), c["max_len"]})
             ctx.set_policy(cuts, predict=c["policy"] == "predict")
         if c["mode"] in ("pageable", "pageable_in_place"):
