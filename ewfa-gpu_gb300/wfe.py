@@ -406,7 +406,7 @@ class Server:
 
     def __init__(self, max_seq_len: int, cigar_stride: int = 0, max_distance: int = 0, lanes: int = 0,
                  batch_pairs: int = 0, memory_bytes: int = 0, bucket_max_len=None, first_tier=None,
-                 predict: bool = False, device: int = 0):
+                 predict: bool = False, device: int = 0, bound: bool = True):
         cfg = ServerConfig()
         cfg.device, cfg.max_seq_len, cfg.cigar_stride, cfg.max_distance = device, max_seq_len, cigar_stride, \
             max_distance
@@ -416,7 +416,7 @@ class Server:
             for i, m in enumerate(bucket_max_len):
                 cfg.bucket_max_len[i] = m
                 cfg.first_tier[i] = -1 if first_tier is None else first_tier[i]
-        cfg.policy_flags = POLICY_PREDICT if predict else 0
+        cfg.policy_flags = (POLICY_PREDICT if predict else 0) | (0 if bound else POLICY_NO_BOUND)
         h = C.c_void_p()
         _check(load().wfe_server_create(C.byref(cfg), C.byref(h)), "wfe_server_create")
         self._h = h
