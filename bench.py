@@ -47,7 +47,7 @@ METRIC = "alignments/sec"
 # seed, committed ncu summary of the dominant kernel
 THROUGHPUT = {
     "short": (1_000_000, 100_000, 150, 0.05, 2, "tier0_short_reads.txt"),
-    "long": (200_000, 20_000, 1000, 0.10, 3, "tier2_long_reads.txt"),
+    "long": (200_000, 20_000, 1000, 0.10, 3, "tier5_long_reads.txt"),
 }
 
 

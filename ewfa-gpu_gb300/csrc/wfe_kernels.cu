@@ -622,7 +622,7 @@ __global__ void long_kernel(const __grid_constant__ AlignLaunch A)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr int kW = NT / 32;
-    static_assert(kW >= 2, "warps 0 and 1 load the two sequences");
+    static_assert(kW >= 1, "at least one warp");
     const bool in_class = A.cls >= 0;
     const TierShape& sh = in_class ? A.chain.cls.shape[A.cls] : A.chain.shape[A.tier];
     const int dlim = sh.dlim;
@@ -663,8 +663,9 @@ __global__ void long_kernel(const __grid_constant__ AlignLaunch A)
         int state = !pr.in_range ? ST_RANGE : (mx > A.max_len || mx > 16u * seq_words) ? ST_TOOLONG : ST_RUN;
         const int plen = state == ST_RUN ? (int)pr.plen : 0, tlen = state == ST_RUN ? (int)pr.tlen : 0;
         const int kt = tlen - plen;
+        /* warps 0 and 1 load the two sequences (warp 0 both, in a one-warp CTA) */
         if (warp == 0) load_packed<32, 4>(pr.p, (uint32_t)plen, QP, lane, kFull);
-        if (warp == 1) load_packed<32, 4>(pr.t, (uint32_t)tlen, QT, lane, kFull);
+        if (warp == (kW > 1 ? 1 : 0)) load_packed<32, 4>(pr.t, (uint32_t)tlen, QT, lane, kFull);
         __syncthreads();
         int D = 0;
         /* last step: the tier's limit or the caller's cap */

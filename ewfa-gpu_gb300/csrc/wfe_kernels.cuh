@@ -48,13 +48,13 @@ struct TierShape {
  * two to three times the pairs in flight per SM of one launch sized for
  * distance 2047.  Limits 255, 511 and 1023, each kept only while below half
  * of tier 5's own limit, then tier 5's own limit (min(max_len, 2047)).
- * Classes up to distance 255 run CTAs of 64 threads, up to 1024 of 128, the
- * last one (when larger) 256: a pair of short distance has few cells per
- * step to share, and fewer warps per pair spend fewer instructions on each
- * step's bookkeeping and barrier. */
+ * Class 255 runs CTAs of one warp, classes up to distance 1024 CTAs of 128
+ * threads, the last one (when larger) 256: a pair of short distance has few
+ * cells per step to share, and fewer warps per pair spend fewer instructions
+ * on each step's bookkeeping and barrier. */
 constexpr int kLongClasses = 4;
 constexpr int kLongClassLimit[kLongClasses - 1] = {255, 511, 1023};
-constexpr int kLongTinyThreads = 64;
+constexpr int kLongTinyThreads = 32;
 constexpr int kLongTinyDistance = 255;   /* classes up to this limit use kLongTinyThreads */
 constexpr int kLongSmallThreads = 128;
 constexpr int kLongSmallDistance = 1024; /* classes up to this limit use kLongSmallThreads */

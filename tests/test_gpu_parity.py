@@ -228,6 +228,7 @@ def test_two_stages_in_the_scratch_tiers():
     torch_cuda()
     ascii, pairs = wfe.generate(3000, 300, 2600, p_min=0.2, p_max=0.45, seed=41)
     with wfe.Context(max_seq_len=2700, batch_size=150, cigar_stride=3000) as ctx:
+        ctx.set_policy([2700], [3])  # the register tiers first, so that chains pass through 3-6
         d1, c1, s1 = ctx.align(ascii, pairs)
         st = ctx.stats()
         assert st["batches"] == 20 and st["tier_passed"][3] > 0 and st["tier_passed"][4] > 0, st
@@ -255,6 +256,7 @@ def test_device_call_of_several_batches_on_two_streams():
         d_st = torch.full((n,), 255, dtype=torch.uint8, device="cuda")
         s = torch.cuda.Stream()
         with wfe.Context(max_seq_len=2700, batch_size=150, cigar_stride=stride, flags=flags) as ctx:
+            ctx.set_policy([2700], [3])  # chains through the scratch tiers 3-6
             for _ in range(2):
                 ctx.align_device(d_ascii, d_pairs, n, 2700, d_dist, d_cg, d_st, s)
                 with torch.cuda.stream(s):
@@ -578,6 +580,7 @@ def test_long_tiers_without_distance_limit():
     distance 2047 (tier 5), global-memory wavefront beyond (tier 6)."""
     ascii, pairs = _long_tier_pairs()
     with wfe.Context(max_seq_len=5000, cigar_stride=12000) as ctx:
+        ctx.set_policy([5000], [3])  # handed on from the register tiers, through the bound pass
         dist, cg, st = ctx.align(ascii, pairs)
         stats = ctx.stats()
     assert dist.max() > 2047
@@ -592,8 +595,10 @@ def test_long_tiers_in_one_slab_each():
     torch_cuda()
     ascii, pairs = _long_tier_pairs()
     with wfe.Context(max_seq_len=5000, cigar_stride=12000) as ctx:
+        ctx.set_policy([5000], [3])
         want = ctx.align(ascii, pairs)
     with wfe.Context(max_seq_len=5000, cigar_stride=12000, long_scratch=(1, 1)) as ctx:
+        ctx.set_policy([5000], [3])
         got = ctx.align(ascii, pairs)
         stats = ctx.stats()
     assert stats["tier_passed"][4] > 0 and stats["tier_passed"][5] > 0, stats
