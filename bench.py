@@ -244,7 +244,8 @@ def run_mixed(args) -> int:
     """Uneven sizes: lengths log-uniform in [100, 10,000], edit probability
     uniform in [0.01, 0.15].  The same device-resident pairs are aligned
     (1) with the plain fixed-shape launches: one launch shape for every pair,
-        sized for the longest sequence, and
+        sized for the longest sequence (no length buckets, and the CTA-per-pair
+        tier as one launch: no distance bounds, no distance classes), and
     (2) with length buckets: pairs sorted by length on the device, each
         bucket aligned with shapes sized to it, first tiers chosen by the
         autotuner on a sample, and
@@ -273,7 +274,9 @@ def run_mixed(args) -> int:
                          flags=wfe.FLAG_KERNEL_TIMING) as ctx:
             tiers = None
             t_tune = 0.0
-            if mode != "plain":
+            if mode == "plain":
+                ctx.set_policy([max_seq], bound=False)
+            else:
                 t0 = time.perf_counter()
                 tiers = ctx.autotune(d_ascii, d_pairs, n, MIXED_BUCKETS, cache, predict=mode == "predicted")
                 t_tune = time.perf_counter() - t0
