@@ -113,8 +113,19 @@ struct wfe_ctx {
                                                   for host calls, stage 1's own tier scratch */
     int lists_buckets = 1;                     /* length buckets the stages' work lists have room for */
     uint32_t* d_lists_ext = nullptr;           /* work lists of more buckets (wfe_set_policy) */
+    /* The global scratch of tiers 2-6 (both stages') is a second allocation,
+     * made when a call first needs it (deep_ready): until then host calls
+     * run their chains as far as tier 1 and defer the pairs that go further
+     * (see finish_deferred).  Short reads never reach tier 2, and a context
+     * for them holds ~10 MB instead of ~200. */
+    bool deep_ready = false;
+    unsigned char* d_deep = nullptr;
+    bool defer_dirty = false;                  /* a host call with a cut chain did not finish */
+    uint32_t* d_defer = nullptr;               /* deferred pairs (index in the call) */
+    uint32_t* d_defer_count = nullptr;
+    uint32_t defer_cap = 0;
     unsigned char* d_ops_scratch = nullptr;    /* tiers 2-4 backtrace stores */
-    size_t ops_scratch_bytes = 0;
+    size_t ops_scratch_bytes = 0;              /* their size (also before they are allocated) */
     unsigned char* d_long_scratch[kNumTiers] = {}; /* tiers 5-6 slabs */
     uint64_t long_slab[kNumTiers] = {};
     unsigned long long* d_passed = nullptr;    /* pairs each tier handed on, running total */
@@ -157,14 +168,21 @@ int fail_cuda(wfe_ctx* ctx, cudaError_t e)
  * the work in question has completed. */
 int pop_launch_error(wfe_ctx* ctx)
 {
-    volatile uint64_t* f = reinterpret_cast<volatile uint64_t*>(ctx->h_launch_error);
-    if (!f || *f == 0u) return WFE_OK;
-    *f = 0u;
-    return fail_cuda(ctx, cudaErrorLaunchFailure);
+    volatile uint8_t* f = ctx->h_launch_error;
+    if (!f) return WFE_OK;
+    bool failed = false;
+    for (int t = 0; t < kNumTiers; ++t)
+        if (f[t]) {
+            failed = true;
+            f[t] = 0u;
+        }
+    return failed ? fail_cuda(ctx, cudaErrorLaunchFailure) : WFE_OK;
 }
 
-constexpr size_t kLaunchErrorBytes = 8; /* byte t: a device-side launch of tier t failed */
-static_assert(kNumTiers <= (int)kLaunchErrorBytes, "one launch-error byte per tier");
+/* byte t < kNumTiers: a device-side launch of tier t failed; byte
+ * kDeferByte: a chain cut short deferred pairs */
+constexpr size_t kLaunchErrorBytes = 8;
+static_assert(kDeferByte < (int)kLaunchErrorBytes, "one launch-error byte per tier and the deferral byte");
 
 void free_launch_error(wfe_ctx* ctx)
 {
@@ -249,6 +267,45 @@ bool bucket_usable(const BucketPlan& b)
     return true;
 }
 
+/* The global scratch of tiers 2-6 (wfe_ctx::deep_ready): tiers 2-4's
+ * backtrace stores and tiers 5-6's slabs, and, for a context whose host
+ * calls keep two batches in flight, stage 1's own copy of both, in one
+ * allocation.  The buckets' launch plans are made again with it.  The
+ * chains enqueued before it all ended at tier 1, so none used it. */
+int ensure_deep(wfe_ctx* ctx)
+{
+    if (ctx->deep_ready) return WFE_OK;
+    const bool two = !(ctx->cfg.flags & (WFE_FLAG_DEVICE_ONLY | WFE_FLAG_NO_PIPELINE));
+    const int copies = two ? 2 : 1;
+    Carve k;
+    size_t ops_at[2] = {}, long_at[2][kNumTiers] = {}; /* + 1: 0 means none */
+    for (int i = 0; i < copies; ++i) {
+        if (ctx->ops_scratch_bytes) ops_at[i] = k.take(ctx->ops_scratch_bytes) + 1u;
+        for (int t = 5; t < kNumTiers; ++t)
+            if (ctx->long_slab[t] && ctx->scratch_ctas[t])
+                long_at[i][t] = k.take((size_t)ctx->long_slab[t] * (size_t)ctx->scratch_ctas[t]) + 1u;
+    }
+    if (k.used) {
+        unsigned char* p = nullptr;
+        const cudaError_t e = cudaMalloc(&p, k.used);
+        if (e != cudaSuccess) return fail_cuda(ctx, e);
+        ctx->d_deep = p;
+        if (ops_at[0]) ctx->d_ops_scratch = p + (ops_at[0] - 1u);
+        for (int t = 5; t < kNumTiers; ++t)
+            if (long_at[0][t]) ctx->d_long_scratch[t] = p + (long_at[0][t] - 1u);
+        if (two) {
+            Stage& s1 = ctx->st[1];
+            if (ops_at[1]) s1.own_ops_scratch = p + (ops_at[1] - 1u);
+            for (int t = 5; t < kNumTiers; ++t)
+                if (long_at[1][t]) s1.own_long_scratch[t] = p + (long_at[1][t] - 1u);
+        }
+    }
+    if (two) ctx->st[1].own_scratch = true;
+    ctx->deep_ready = true;
+    for (int b = 0; b < ctx->nbuckets; ++b) plan_bucket(ctx, ctx->bucket[b]);
+    return WFE_OK;
+}
+
 TimedLaunch* begin_timing(wfe_ctx* ctx, int t, cudaStream_t s, int* rc)
 {
     *rc = WFE_OK;
@@ -278,12 +335,26 @@ int chain_end(const wfe_config& c, int first, int last)
     return last;
 }
 
+/* Last tier of a chain while the context has no scratch for tiers 2-6:
+ * the chain stops there and defers the pairs it would hand on. */
+constexpr int kShallowLastTier = 1;
+
+/* Last tier a chain from `first` runs to now (see chain_end and
+ * kShallowLastTier), and whether that cuts it short. */
+int chain_last(const wfe_ctx* ctx, int first, int last, bool* cut)
+{
+    const int end = chain_end(ctx->cfg, first, last);
+    *cut = !ctx->deep_ready && end > kShallowLastTier;
+    return *cut ? kShallowLastTier : end;
+}
+
 /* Launch the first tier of one bucket's chain over `work` (NULL: pairs
  * 0..n-1); the last CTA of every tier starts the next tier with work, on the
- * device. */
+ * device.  `base` is the index of the batch's first pair in the call (the
+ * deferred pairs of a chain cut short are recorded by it). */
 int launch_bucket(wfe_ctx* ctx, Stage& st, const BucketPlan& bp, int bucket_index, int first_tier,
                   const Layout& L, bool listed, uint32_t n, int32_t* dist, int8_t* cigar, uint8_t* status,
-                  cudaStream_t s)
+                  cudaStream_t s, uint32_t base)
 {
     const wfe_config& c = ctx->cfg;
     const uint32_t B = c.batch_size;
@@ -304,7 +375,9 @@ int launch_bucket(wfe_ctx* ctx, Stage& st, const BucketPlan& bp, int bucket_inde
     a.ops_scratch = st.own_ops_scratch ? st.own_ops_scratch : ctx->d_ops_scratch;
     a.ops_scratch_bytes = ctx->ops_scratch_bytes;
     a.tier = t;
-    const int last = chain_end(c, t, bp.last_tier);
+    bool cut = false;
+    const int last = chain_last(ctx, t, bp.last_tier, &cut);
+    if (t > last) return WFE_ERR_INTERNAL; /* a first tier past 1 gets its scratch before it launches */
     a.chain.last_tier = last;
     for (int u = 0; u < kNumTiers; ++u) {
         a.chain.shape[u] = bp.shape[u];
@@ -317,8 +390,14 @@ int launch_bucket(wfe_ctx* ctx, Stage& st, const BucketPlan& bp, int bucket_inde
     a.chain.launched = ctx->d_launched;
     a.chain.passed = ctx->d_passed;
     a.chain.launch_error = ctx->d_launch_error;
-    a.retry = t < last ? a.chain.list[t + 1] : nullptr;
-    a.retry_count = words + t + 1;
+    if (cut) {
+        a.chain.defer = ctx->d_defer;
+        a.chain.defer_count = ctx->d_defer_count;
+        a.chain.defer_cap = ctx->defer_cap;
+        a.chain.defer_base = base;
+    }
+    a.retry = t < last ? a.chain.list[t + 1] : a.chain.defer;
+    a.retry_count = t < last ? words + t + 1 : a.chain.defer_count;
     a.passed_total = ctx->d_passed + t;
     a.cls = -1;
     /* Distance bounds (and with them tier 5's classes) for every chain that
@@ -373,7 +452,7 @@ int launch_bucket(wfe_ctx* ctx, Stage& st, const BucketPlan& bp, int bucket_inde
  * shapes fit its longest sequence, and by predicted distance to a tier --
  * and every bucket's chain runs from its first tier. */
 int run_chain(wfe_ctx* ctx, Stage& st, const Layout& L, uint32_t n, int32_t* dist, int8_t* cigar,
-              uint8_t* status, cudaStream_t s, const int* first_override = nullptr)
+              uint8_t* status, cudaStream_t s, const int* first_override = nullptr, uint32_t base = 0)
 {
     if (n == 0) return WFE_OK;
     const uint32_t B = ctx->cfg.batch_size;
@@ -382,7 +461,7 @@ int run_chain(wfe_ctx* ctx, Stage& st, const Layout& L, uint32_t n, int32_t* dis
         const BucketPlan& bp = ctx->bucket[0];
         const int t = first_override ? first_override[0] : bp.first_tier;
         ctx->single_entered[t] += n;
-        return launch_bucket(ctx, st, bp, 0, t, L, false, n, dist, cigar, status, s);
+        return launch_bucket(ctx, st, bp, 0, t, L, false, n, dist, cigar, status, s, base);
     }
     Buckets bk{};
     bk.n = ctx->nbuckets;
@@ -390,7 +469,8 @@ int run_chain(wfe_ctx* ctx, Stage& st, const Layout& L, uint32_t n, int32_t* dis
         bk.max_len[b] = ctx->bucket[b].max_len;
         bk.first_tier[b] = first_override ? first_override[b] : ctx->bucket[b].first_tier;
         /* routing never goes past the end of the bucket's chain */
-        bk.last_tier[b] = chain_end(ctx->cfg, bk.first_tier[b], ctx->bucket[b].last_tier);
+        bool cut = false;
+        bk.last_tier[b] = chain_last(ctx, bk.first_tier[b], ctx->bucket[b].last_tier, &cut);
     }
     for (int t = 0; t < kNumTiers; ++t) bk.dcap[t] = tier_info(t).dcap;
     /* predictions only move pairs of buckets that start below tier 5 */
@@ -411,7 +491,8 @@ int run_chain(wfe_ctx* ctx, Stage& st, const Layout& L, uint32_t n, int32_t* dis
     ctx->stats.kernel_launches++;
     /* longest bucket first: its chains take longest */
     for (int b = ctx->nbuckets - 1; b >= 0; --b) {
-        const int r = launch_bucket(ctx, st, ctx->bucket[b], b, bk.first_tier[b], L, true, n, dist, cigar, status, s);
+        const int r =
+            launch_bucket(ctx, st, ctx->bucket[b], b, bk.first_tier[b], L, true, n, dist, cigar, status, s, base);
         if (r != WFE_OK) return r;
     }
     return WFE_OK;
@@ -474,6 +555,7 @@ int create_context(const wfe_config* cfg, uint64_t budget5, uint64_t budget6, wf
         cudaGetLastError(); /* reported here, not to a later call */
         for (auto& s : ctx->st) free_stage(s);
         cudaFree(ctx->d_arena);
+        cudaFree(ctx->d_deep);
         free_launch_error(ctx);
         delete ctx;
         return err == cudaErrorMemoryAllocation ? WFE_ERR_OUT_OF_MEMORY : WFE_ERR_CUDA;
@@ -487,10 +569,12 @@ int create_context(const wfe_config* cfg, uint64_t budget5, uint64_t budget6, wf
     ctx->host_page_tables = hpt != 0;
     /* Global scratch is sized for the longest sequences (max_seq_len); a
      * bucket of shorter sequences has more resident CTAs and uses at most
-     * the CTAs that scratch was sized for.  Everything the context keeps on
-     * the device is carved from one allocation. */
+     * the CTAs that scratch was sized for.  Tiers 2-6's scratch is one
+     * allocation (ensure_deep), made here when the first tier is past 1 or
+     * the context is for device calls only, else by the first call that
+     * needs it; everything else the context keeps on the device is carved
+     * from another. */
     size_t scratch = 0;
-    size_t long_at[kNumTiers] = {};
     Carve arena;
     const int last = c.max_seq_len > (uint32_t)kLongSmemDistance ? 6 : 5;
     for (int t = 0; t <= last; ++t) {
@@ -506,10 +590,9 @@ int create_context(const wfe_config* cfg, uint64_t budget5, uint64_t budget6, wf
             const int grid = (int)std::min<uint64_t>((uint64_t)sh.grid, std::max<uint64_t>(1, budget / sh.slab));
             ctx->scratch_ctas[t] = grid;
             ctx->long_slab[t] = sh.slab;
-            long_at[t] = arena.take((size_t)sh.slab * grid) + 1u; /* + 1: 0 means none */
         }
     }
-    const size_t ops_at = scratch ? arena.take(scratch) : 0u;
+    ctx->ops_scratch_bytes = scratch;
     const size_t nctr = 2 * kNumTiers + kMaxBuckets;
     const size_t passed_at = arena.take(sizeof(unsigned long long) * nctr);
     const size_t B = c.batch_size;
@@ -522,26 +605,14 @@ int create_context(const wfe_config* cfg, uint64_t budget5, uint64_t budget6, wf
         pred_at[i] = arena.take(B * sizeof(uint16_t));
         bound_at[i] = arena.take(B * sizeof(int32_t));
     }
-    /* Host calls of several batches keep two in flight, and the second
-     * stage then needs its own tier scratch: reserve it now, in the same
-     * allocation, rather than in the middle of the first such call.  (A
-     * device-only context allocates it at its first device call of several
-     * batches; see ensure_stage_scratch.) */
-    const bool host_pipeline = !(c.flags & (WFE_FLAG_DEVICE_ONLY | WFE_FLAG_NO_PIPELINE));
-    size_t own_ops_at = 0, own_long_at[kNumTiers] = {};
-    if (host_pipeline) {
-        if (scratch) own_ops_at = arena.take(scratch);
-        for (int t = 5; t < kNumTiers; ++t)
-            if (long_at[t]) own_long_at[t] = arena.take((size_t)ctx->long_slab[t] * ctx->scratch_ctas[t]) + 1u;
-    }
+    /* pairs deferred by host calls that run before tiers 2-6 have scratch */
+    const size_t defer_at = arena.take(B * sizeof(uint32_t));
+    const size_t defer_count_at = arena.take(sizeof(uint32_t));
     if ((e = cudaMalloc(&ctx->d_arena, arena.used)) != cudaSuccess) return bail(e);
     unsigned char* A0 = ctx->d_arena;
-    for (int t = 5; t < kNumTiers; ++t)
-        if (long_at[t]) ctx->d_long_scratch[t] = A0 + (long_at[t] - 1u);
-    if (scratch) {
-        ctx->d_ops_scratch = A0 + ops_at;
-        ctx->ops_scratch_bytes = scratch;
-    }
+    ctx->d_defer = reinterpret_cast<uint32_t*>(A0 + defer_at);
+    ctx->d_defer_count = reinterpret_cast<uint32_t*>(A0 + defer_count_at);
+    ctx->defer_cap = (uint32_t)B;
     ctx->d_passed = reinterpret_cast<unsigned long long*>(A0 + passed_at);
     for (int i = 0; i < kStages; ++i) {
         Stage& s = ctx->st[i];
@@ -549,13 +620,6 @@ int create_context(const wfe_config* cfg, uint64_t budget5, uint64_t budget6, wf
         s.d_counts = reinterpret_cast<uint32_t*>(A0 + counts_at[i]);
         s.d_pred = reinterpret_cast<uint16_t*>(A0 + pred_at[i]);
         s.d_bound = reinterpret_cast<int32_t*>(A0 + bound_at[i]);
-    }
-    if (host_pipeline) {
-        Stage& s1 = ctx->st[1];
-        if (scratch) s1.own_ops_scratch = A0 + own_ops_at;
-        for (int t = 5; t < kNumTiers; ++t)
-            if (own_long_at[t]) s1.own_long_scratch[t] = A0 + (own_long_at[t] - 1u);
-        s1.own_scratch = true;
     }
     ctx->nbuckets = 1;
     ctx->bucket[0].max_len = c.max_seq_len;
@@ -592,7 +656,11 @@ int create_context(const wfe_config* cfg, uint64_t budget5, uint64_t budget6, wf
     /* the counters start at zero; both stages' streams come after this */
     if ((e = cudaMemsetAsync(ctx->d_passed, 0, sizeof(unsigned long long) * nctr, ctx->st[0].stream)) != cudaSuccess)
         return bail(e);
+    if ((e = cudaMemsetAsync(ctx->d_defer_count, 0, sizeof(uint32_t), ctx->st[0].stream)) != cudaSuccess)
+        return bail(e);
     if ((e = cudaStreamSynchronize(ctx->st[0].stream)) != cudaSuccess) return bail(e);
+    if ((c.flags & WFE_FLAG_DEVICE_ONLY) || ctx->bucket[0].first_tier > kShallowLastTier)
+        if (ensure_deep(ctx) != WFE_OK) return bail((cudaError_t)ctx->last_cuda_error);
     *out = ctx;
     return WFE_OK;
 }
@@ -632,6 +700,14 @@ int wfe_set_policy(wfe_ctx* ctx, uint32_t nbuckets, const uint32_t* bucket_max_l
     }
     WFE_CUDA(ctx, cudaSetDevice(ctx->cfg.device));
     for (auto& s : ctx->st) WFE_CUDA(ctx, cudaStreamSynchronize(s.stream));
+    /* a first tier past 1, or routing by predicted distance, needs tiers
+     * 2-6's scratch from the start */
+    bool deep = (flags & WFE_POLICY_PREDICT) != 0;
+    for (uint32_t b = 0; b < nbuckets; ++b) deep |= plan[b].first_tier > kShallowLastTier;
+    if (deep && !ctx->deep_ready) {
+        if (const int r = ensure_deep(ctx)) return r;
+        for (uint32_t b = 0; b < nbuckets; ++b) plan_bucket(ctx, plan[b]);
+    }
     if ((int)nbuckets > ctx->lists_buckets) {
         /* work lists for every tier of every bucket, both stages */
         const size_t per_stage = (size_t)nbuckets * kListsPerBucket * ctx->cfg.batch_size;
@@ -670,6 +746,7 @@ void wfe_destroy(wfe_ctx* ctx)
         if (s.stream) cudaStreamSynchronize(s.stream);
     for (auto& s : ctx->st) free_stage(s);
     cudaFree(ctx->d_arena);
+    cudaFree(ctx->d_deep);
     cudaFree(ctx->d_lists_ext);
     free_launch_error(ctx);
     for (auto& t : ctx->timed) {
@@ -731,6 +808,9 @@ int wfe_align_device(wfe_ctx* ctx, const char* d_ascii, const wfe_pair* d_pairs,
     WFE_CUDA(ctx, cudaSetDevice(ctx->cfg.device));
     /* an earlier asynchronous call whose device-side launch failed */
     if (const int r = pop_launch_error(ctx)) return r;
+    /* a device call returns before its chains end, so they run whole: the
+     * first one allocates tiers 2-6's scratch if no call has yet */
+    if (const int r = ensure_deep(ctx)) return r;
     cudaStream_t s = stream ? (cudaStream_t)stream : ctx->st[0].stream;
     const size_t B = ctx->cfg.batch_size;
     /* Several batches alternate between `stream` (stage 0) and stage 1's
@@ -982,11 +1062,13 @@ int ensure_staging(wfe_ctx* ctx, Stage& s)
 }
 
 /* Stage 1's own scratch of tiers 2-6, the size of the context's, allocated
- * when a host call first runs two batches at once.  A failed allocation
+ * when a device call first runs two batches at once on a context for
+ * device calls only (other contexts get it with the context's, in
+ * ensure_deep; before that their chains need none).  A failed allocation
  * leaves none of it behind. */
 int ensure_stage_scratch(wfe_ctx* ctx, Stage& s)
 {
-    if (s.own_scratch) return WFE_OK;
+    if (s.own_scratch || !ctx->deep_ready) return WFE_OK;
     Carve c;
     const size_t ops_at = ctx->d_ops_scratch ? c.take(ctx->ops_scratch_bytes) : 0u;
     size_t long_at[kNumTiers] = {};
@@ -1009,6 +1091,8 @@ int ensure_stage_scratch(wfe_ctx* ctx, Stage& s)
 
 int align_host_checked(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, int8_t* cigar_out,
                        uint8_t* status_out);
+int finish_deferred(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, int8_t* cigar_out,
+                    uint8_t* status_out);
 
 /* The host-buffer calls: no C++ exception crosses the C ABI. */
 int align_host(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, int8_t* cigar_out,
@@ -1030,6 +1114,24 @@ int align_host_checked(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist
     if (c.flags & WFE_FLAG_DEVICE_ONLY) return WFE_ERR_INVALID_ARGUMENT;
     WFE_CUDA(ctx, cudaSetDevice(c.device));
     const bool want_cigar = cigar_out && c.cigar_stride;
+    if (!ctx->deep_ready) {
+        /* Without tiers 2-6's scratch the chains stop at tier 1 and defer
+         * what they would hand on, recorded by the pair's index in the call.
+         * A first tier past 1, or more pairs than those indices hold, needs
+         * the scratch now. */
+        bool deep = n > (size_t)UINT32_MAX;
+        for (int b = 0; b < ctx->nbuckets; ++b) deep |= ctx->bucket[b].first_tier > kShallowLastTier;
+        if (deep) {
+            if (const int r = ensure_deep(ctx)) return r;
+        } else {
+            if (ctx->defer_dirty) {
+                /* an earlier call that deferred pairs did not finish */
+                WFE_CUDA(ctx, cudaMemset(ctx->d_defer_count, 0, sizeof(uint32_t)));
+                reinterpret_cast<volatile uint8_t*>(ctx->h_launch_error)[kDeferByte] = 0u;
+            }
+            ctx->defer_dirty = true;
+        }
+    }
 
     /* pinned inputs are read in place, pinned outputs written in place, and
      * so are pageable ones when asked for on a device that can */
@@ -1162,10 +1264,11 @@ int align_host_checked(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist
             out_pages.ready(bi);
             const int r = run_chain(ctx, st, L, (uint32_t)nb, m_dist + b0,
                                     want_cigar ? m_cigar + b0 * c.cigar_stride : nullptr,
-                                    status_out ? m_status + b0 : nullptr, s);
+                                    status_out ? m_status + b0 : nullptr, s, nullptr, (uint32_t)b0);
             if (r != WFE_OK) return r;
         } else {
-            const int r = run_chain(ctx, st, L, (uint32_t)nb, st.d_dist, st.d_cigar, st.d_status, s);
+            const int r = run_chain(ctx, st, L, (uint32_t)nb, st.d_dist, st.d_cigar, st.d_status, s, nullptr,
+                                    (uint32_t)b0);
             if (r != WFE_OK) return r;
             WFE_CUDA(ctx, cudaMemcpyAsync(dist_out + b0, st.d_dist, nb * 4u, cudaMemcpyDeviceToHost, s));
             ctx->stats.d2h_bytes += nb * 4u;
@@ -1183,7 +1286,66 @@ int align_host_checked(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist
         ctx->stats.pairs += nb;
     }
     for (int i = 0; i < nstages; ++i) WFE_CUDA(ctx, cudaStreamSynchronize(ctx->st[i].stream));
-    return pop_launch_error(ctx);
+    if (const int r = pop_launch_error(ctx)) return r;
+    if (ctx->defer_dirty) {
+        if (reinterpret_cast<volatile uint8_t*>(ctx->h_launch_error)[kDeferByte])
+            return finish_deferred(ctx, job, n, dist_out, cigar_out, status_out);
+        ctx->defer_dirty = false; /* nothing deferred, the count is still 0 */
+    }
+    return WFE_OK;
+}
+
+/* A host call whose chains stopped at tier 1 deferred some pairs: allocate
+ * tiers 2-6's scratch, then align those pairs as a call of their own (from
+ * tier 0 again: a few of a call's pairs at most, as a rule) and put their
+ * results in place.  When more were deferred than the list holds, the
+ * whole call runs again. */
+int finish_deferred(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_out, int8_t* cigar_out,
+                    uint8_t* status_out)
+{
+    const wfe_config& c = ctx->cfg;
+    uint32_t cnt = 0;
+    WFE_CUDA(ctx, cudaMemcpy(&cnt, ctx->d_defer_count, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    std::vector<uint32_t> idx;
+    if (cnt <= ctx->defer_cap) {
+        idx.resize(cnt);
+        if (cnt) WFE_CUDA(ctx, cudaMemcpy(idx.data(), ctx->d_defer, cnt * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    }
+    WFE_CUDA(ctx, cudaMemset(ctx->d_defer_count, 0, sizeof(uint32_t)));
+    reinterpret_cast<volatile uint8_t*>(ctx->h_launch_error)[kDeferByte] = 0u;
+    ctx->defer_dirty = false;
+    if (const int r = ensure_deep(ctx)) return r;
+    if (cnt > ctx->defer_cap) return align_host_checked(ctx, job, n, dist_out, cigar_out, status_out);
+    std::vector<wfe_pair> sub(cnt);
+    for (uint32_t k = 0; k < cnt; ++k) {
+        const uint32_t j = idx[k];
+        if (j >= n) return WFE_ERR_INTERNAL;
+        if (job.pairs) {
+            sub[k] = job.pairs[j];
+        } else {
+            /* the strided layout as descriptors: pattern, then text, in slot j */
+            const uint64_t o = 2ull * j * job.stride;
+            sub[k].p_off = o;
+            sub[k].t_off = o + job.stride;
+            sub[k].p_len = job.p_len[j];
+            sub[k].t_len = job.t_len[j];
+        }
+    }
+    const size_t stride = c.cigar_stride;
+    const bool want_cigar = cigar_out && stride;
+    std::vector<int32_t> d(cnt);
+    std::vector<int8_t> cg(want_cigar ? (size_t)cnt * stride : 0u);
+    std::vector<uint8_t> st(cnt);
+    const HostJob sj{job.ascii, job.ascii_bytes, sub.data(), 0, nullptr, nullptr};
+    if (const int r = align_host_checked(ctx, sj, cnt, d.data(), want_cigar ? cg.data() : nullptr, st.data()))
+        return r;
+    for (uint32_t k = 0; k < cnt; ++k) {
+        const uint32_t j = idx[k];
+        dist_out[j] = d[k];
+        if (want_cigar) std::memcpy(cigar_out + (size_t)j * stride, cg.data() + (size_t)k * stride, stride);
+        if (status_out) status_out[j] = st[k];
+    }
+    return WFE_OK;
 }
 
 }  // namespace
@@ -1359,6 +1521,8 @@ extern "C" int wfe_autotune(wfe_ctx* ctx, const char* d_ascii, const wfe_pair* d
      * through the same routing and chains as a real batch */
     int r = wfe_set_policy(ctx, nbuckets, bucket_max_len, nullptr, flags);
     if (r != WFE_OK) return r;
+    /* the trials start chains at every tier */
+    if ((r = ensure_deep(ctx)) != WFE_OK) return r;
     constexpr size_t kSample = 4096;
     const size_t ns = std::min<size_t>(n, std::max<size_t>(kSample * nbuckets, 65536));
     std::vector<wfe_pair> host(ns);

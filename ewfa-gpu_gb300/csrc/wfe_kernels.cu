@@ -204,6 +204,17 @@ __device__ __forceinline__ void note_launch_error(const AlignLaunch& A, int u)
     }
 }
 
+/* Pairs of a chain cut short were deferred: the host aligns them once the
+ * deeper tiers' scratch exists.  (Host memory the device writes in place,
+ * like the launch failures.) */
+__device__ __forceinline__ void note_deferred(const AlignLaunch& A)
+{
+    if (A.chain.launch_error) {
+        *reinterpret_cast<volatile uint8_t*>(A.chain.launch_error + kDeferByte) = 1u;
+        __threadfence_system();
+    }
+}
+
 /* Tail launch of tier u over its list of `count` pairs, built in the launch's
  * own parameter buffer: A (a __grid_constant__ kernel parameter, read in
  * place) is copied word by word and the per-tier fields are patched.  No
@@ -229,8 +240,8 @@ __device__ __forceinline__ void tail_launch(K kernel, const AlignLaunch& A, int 
     n->cls = -1;
     n->work = A.chain.list[u];
     n->work_count = A.chain.counts + u;
-    n->retry = u < A.chain.last_tier ? A.chain.list[u + 1] : nullptr;
-    n->retry_count = A.chain.counts + u + 1;
+    n->retry = u < A.chain.last_tier ? A.chain.list[u + 1] : A.chain.defer;
+    n->retry_count = u < A.chain.last_tier ? A.chain.counts + u + 1 : A.chain.defer_count;
     n->passed_total = A.chain.passed ? A.chain.passed + u : nullptr;
     if (tier_args) {
         uint32_t* extra = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(buf) + sizeof(AlignLaunch));
@@ -550,10 +561,15 @@ __device__ __forceinline__ void tier_body(const AlignLaunch& A, uint32_t seq_wor
                                                                   : (uint8_t)WFE_PAIR_OK;
             }
         } else if (state == ST_OVERFLOW && A.retry) {
-            /* hand the pair to the next tier */
+            /* hand the pair to the next tier, or defer it (a chain cut short) */
             if (g == 0) {
                 const uint32_t s = atomicAdd(A.retry_count, 1u);
-                A.retry[s] = pi;
+                if (A.retry != A.chain.defer) {
+                    A.retry[s] = pi;
+                } else {
+                    if (s < A.chain.defer_cap) A.retry[s] = A.chain.defer_base + pi;
+                    note_deferred(A);
+                }
                 if (A.passed_total) atomicAdd(A.passed_total, 1ull);
             }
         } else if (state == ST_OVERFLOW || state == ST_OVERMAX || state == ST_TOOLONG ||

@@ -99,7 +99,20 @@ struct Chain {
                                         the device writes in place) */
     LongClasses cls;                 /* tier 5's distance classes */
     TierShape bound_shape;           /* the bound pass: grid, smem, seq_words, threads */
+    /* A chain cut short at the last tier that needs no global scratch (the
+     * context has not allocated the scratch of the deeper tiers yet): the
+     * pairs that tier hands on go to defer as defer_base + their index (up
+     * to defer_cap of them; defer_count counts them all), and byte
+     * kDeferByte of launch_error is set, for the host to align them once the
+     * scratch exists.  NULL: the chain is whole. */
+    uint32_t* defer;
+    uint32_t* defer_count;
+    uint32_t defer_cap;
+    uint32_t defer_base;
 };
+/* launch_error byte that says pairs were deferred (bytes 0..kNumTiers-1 are
+ * the tiers' launch failures) */
+constexpr int kDeferByte = kNumTiers;
 
 /* Length buckets of the classify kernel, and for each the tiers a pair may
  * be routed to by its predicted distance. */

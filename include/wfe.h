@@ -132,6 +132,17 @@ typedef struct wfe_stats {
  * inputs and results are allocated by the first host call that stages
  * (buffers used in place never need them); that call returns
  * WFE_ERR_OUT_OF_MEMORY if they do not fit.
+ * The global scratch of tiers 2-6 (distances past 79; tens to hundreds of
+ * MB, for both pipeline stages) is allocated here only for contexts with
+ * WFE_FLAG_DEVICE_ONLY or whose first tier is past 1 (max_seq_len above
+ * 1,200).  Otherwise the first call that needs it allocates it: the first
+ * device call, the first wfe_set_policy or wfe_autotune that starts a chain
+ * past tier 1 or routes by prediction, or the first host call in which a
+ * pair's distance passes 79.  Such a host call aligns those pairs again
+ * once the scratch exists (from their index in the call; when more than
+ * batch_size were deferred, the whole call runs again), with the same
+ * results.  A short-read context that never needs it holds ~10 MB of device
+ * memory instead of ~200 MB, and frees it sooner.
  * Threading: a context is used by one thread at a time; different contexts
  * may be used from different threads at once.  Every call on a context makes
  * its device the calling thread's current device (as the reference's
@@ -270,8 +281,10 @@ int wfe_align_strided(wfe_ctx* ctx, const char* ascii, size_t stride,
  * `stream` and one of the context's -- so that consecutive batches overlap
  * on the device; the context's stream waits for the work already on
  * `stream`, and `stream` waits for it at the end, so the call stays ordered
- * on `stream`.  The first such call allocates the second stream's tier
- * scratch (about as much as wfe_create did; without it the batches run one
+ * on `stream`.  The first device call allocates the scratch of tiers 2-6
+ * if the context has none yet (see wfe_create); on a context with
+ * WFE_FLAG_DEVICE_ONLY the first call of more than batch_size pairs
+ * allocates the second stream's copy of it (without it the batches run one
  * after another; WFE_FLAG_NO_PIPELINE keeps them on `stream` alone).
  * Replaces the kernel chain WF_edit_distance -> generate_cigars
  * (src/wavefront.cu:203-260). */
