@@ -67,8 +67,9 @@ struct Stage {
 };
 
 /* Sub-buffers carved from one device allocation, each 256-byte aligned: a
- * cudaMalloc or cudaFree costs 40-140 us on this path whatever its size, so
- * a context makes one at creation and frees one at teardown. */
+ * cudaMalloc or cudaFree costs 40-140 us on this path (plus ~0.4 us per MB
+ * freed), so a context makes one at creation -- and one more for tiers
+ * 2-6's scratch, when a call first needs it -- and frees them at teardown. */
 struct Carve {
     size_t used = 0;
     size_t take(size_t bytes)
