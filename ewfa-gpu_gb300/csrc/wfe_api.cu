@@ -121,6 +121,7 @@ struct wfe_ctx {
      * for them holds ~10 MB instead of ~200. */
     bool deep_ready = false;
     unsigned char* d_deep = nullptr;
+    size_t deep_bytes = 0;
     bool defer_dirty = false;                  /* a host call with a cut chain did not finish */
     uint32_t* d_defer = nullptr;               /* deferred pairs (index in the call) */
     uint32_t* d_defer_count = nullptr;
@@ -291,6 +292,7 @@ int ensure_deep(wfe_ctx* ctx)
         const cudaError_t e = cudaMalloc(&p, k.used);
         if (e != cudaSuccess) return fail_cuda(ctx, e);
         ctx->d_deep = p;
+        ctx->deep_bytes = k.used;
         if (ops_at[0]) ctx->d_ops_scratch = p + (ops_at[0] - 1u);
         for (int t = 5; t < kNumTiers; ++t)
             if (long_at[0][t]) ctx->d_long_scratch[t] = p + (long_at[0][t] - 1u);
@@ -777,6 +779,7 @@ int wfe_get_stats(wfe_ctx* ctx, wfe_stats* out)
     unsigned long long dev[2 * kNumTiers + kMaxBuckets] = {};
     WFE_CUDA(ctx, cudaMemcpy(dev, ctx->d_passed, sizeof(dev), cudaMemcpyDeviceToHost));
     *out = ctx->stats;
+    out->deep_scratch_bytes = ctx->deep_bytes;
     for (int t = 0; t < kNumTiers; ++t) {
         out->tier_passed[t] = dev[t];
         out->tier_entered[t] = ctx->single_entered[t] + (t > 0 ? dev[t - 1] : 0);
@@ -1316,6 +1319,7 @@ int finish_deferred(wfe_ctx* ctx, const HostJob& job, size_t n, int32_t* dist_ou
     reinterpret_cast<volatile uint8_t*>(ctx->h_launch_error)[kDeferByte] = 0u;
     ctx->defer_dirty = false;
     if (const int r = ensure_deep(ctx)) return r;
+    ctx->stats.deferred_pairs += cnt;
     if (cnt > ctx->defer_cap) return align_host_checked(ctx, job, n, dist_out, cigar_out, status_out);
     std::vector<wfe_pair> sub(cnt);
     for (uint32_t k = 0; k < cnt; ++k) {

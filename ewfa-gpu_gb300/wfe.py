@@ -60,7 +60,8 @@ class Stats(C.Structure):
     _fields_ = [("pairs", C.c_uint64), ("batches", C.c_uint64), ("kernel_launches", C.c_uint64),
                 ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("tier_entered", C.c_uint64 * 8),
                 ("tier_passed", C.c_uint64 * 8), ("tier_launches", C.c_uint64 * 8),
-                ("tier_ms", C.c_double * 8), ("mapped_batches", C.c_uint64)]
+                ("tier_ms", C.c_double * 8), ("mapped_batches", C.c_uint64), ("deferred_pairs", C.c_uint64),
+                ("deep_scratch_bytes", C.c_uint64)]
 
 
 class ServerConfig(C.Structure):
@@ -322,7 +323,8 @@ class Context:
                 "h2d_bytes": s.h2d_bytes, "d2h_bytes": s.d2h_bytes,
                 "tier_entered": list(s.tier_entered), "tier_passed": list(s.tier_passed),
                 "tier_launches": list(s.tier_launches), "tier_ms": list(s.tier_ms),
-                "mapped_batches": s.mapped_batches}
+                "mapped_batches": s.mapped_batches, "deferred_pairs": s.deferred_pairs,
+                "deep_scratch_bytes": s.deep_scratch_bytes}
 
     def reset_stats(self) -> None:
         _check(load().wfe_reset_stats(self._h), "wfe_reset_stats")

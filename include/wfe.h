@@ -28,7 +28,8 @@
 extern "C" {
 #endif
 
-#define WFE_ABI_VERSION 2 /* 2: wfe_server_stats gained admit_ns and finish_ns */
+#define WFE_ABI_VERSION 3 /* 2: wfe_server_stats gained admit_ns and finish_ns; 3: wfe_stats gained
+                             deferred_pairs and deep_scratch_bytes */
 
 /* Call status.  The reference exits the process on any CUDA error
  * (utils/cuda_helpers.cuh:24-31) or fatal condition (utils/logger.h:66-68). */
@@ -121,6 +122,11 @@ typedef struct wfe_stats {
     uint64_t mapped_batches;   /* host-call batches whose inputs the kernels
                                   read in place (pinned, or pageable with
                                   WFE_FLAG_PAGEABLE_IN_PLACE) */
+    uint64_t deferred_pairs;   /* pairs a host call deferred past tier 1 and
+                                  aligned again once tiers 2-6 had scratch
+                                  (see wfe_create) */
+    uint64_t deep_scratch_bytes; /* device bytes of tiers 2-6's scratch, both
+                                  stages (0 until a call needs it; not reset) */
 } wfe_stats;
 
 /* ---- lifecycle -------------------------------------------------------- */

@@ -120,7 +120,8 @@ def test_struct_layouts_match_the_header(tmp_path):
     src = tmp_path / "layout.c"
     checks = {
         "wfe_config": (wfe.Config, ["device", "max_seq_len", "batch_size", "max_distance", "cigar_stride", "flags"]),
-        "wfe_stats": (wfe.Stats, ["pairs", "tier_entered", "tier_ms", "mapped_batches"]),
+        "wfe_stats": (wfe.Stats, ["pairs", "tier_entered", "tier_ms", "mapped_batches", "deferred_pairs",
+                                  "deep_scratch_bytes"]),
         "wfe_server_config": (wfe.ServerConfig, ["memory_bytes", "nbuckets", "bucket_max_len", "first_tier",
                                                  "policy_flags"]),
         "wfe_request_info": (wfe.RequestInfo, ["submit_ns", "done_ns", "pairs", "batches"]),

@@ -29,13 +29,14 @@ def strided(ascii, pairs, slot):
 
 @pytest.mark.parametrize("mode", ["pageable", "pageable_in_place", "pinned", "strided"])
 def test_first_host_call_defers_and_realigns(mode):
-    """The first call on a fresh context defers a few hundred of 3,000 pairs
-    (fewer than batch_size) and aligns them again; a second call, with the
+    """The first call on a fresh context defers the 1,336 of 3,000 pairs past
+    distance 79 (fewer than batch_size; two batches, so the indices of the
+    second carry its offset) and aligns them again; a second call, with the
     scratch in place, runs whole chains.  Both match the oracle."""
     torch_cuda()
     ascii, pairs = high_error_pairs(3000, 51)
     flags = wfe.FLAG_PAGEABLE_IN_PLACE if mode == "pageable_in_place" else 0
-    with wfe.Context(max_seq_len=1200, batch_size=1000, cigar_stride=2000, flags=flags) as ctx:
+    with wfe.Context(max_seq_len=1200, batch_size=2000, cigar_stride=2000, flags=flags) as ctx:
         slot = (int(max(pairs["p_len"].max(), pairs["t_len"].max())) + 15) // 16 * 16
 
         def run():
@@ -45,10 +46,15 @@ def test_first_host_call_defers_and_realigns(mode):
             if mode == "pinned":
                 return ctx.align(_pinned(ascii), _pinned(pairs))
             return ctx.align(ascii, pairs)
+        assert ctx.stats()["deep_scratch_bytes"] == 0
         first = run()
         stats = ctx.stats()
         second = run()
+        after = ctx.stats()
     assert first[0].max() > 143 and stats["tier_passed"][1] > 0, stats
+    assert stats["deferred_pairs"] == int((first[0] > 79).sum()) and stats["deep_scratch_bytes"] > 0, stats
+    assert 0 < stats["deferred_pairs"] < 2000, stats
+    assert after["deferred_pairs"] == stats["deferred_pairs"], after  # the second call deferred nothing
     for r in (first, second):
         compare_with_oracle(ascii, pairs, 2000, *r)
 
@@ -61,6 +67,7 @@ def test_more_deferred_pairs_than_the_list_holds():
     ascii, pairs = high_error_pairs(2000, 52)
     with wfe.Context(max_seq_len=1200, batch_size=64, cigar_stride=2000) as ctx:
         got = ctx.align(ascii, pairs)
+        assert ctx.stats()["deferred_pairs"] > 64
     with wfe.Context(max_seq_len=1200, batch_size=64, cigar_stride=2000) as ctx:
         ctx.set_policy([1200], [2])
         want = ctx.align(ascii, pairs)
@@ -86,6 +93,7 @@ def test_short_read_context_holds_little_device_memory():
                      flags=wfe.FLAG_PAGEABLE_IN_PLACE) as ctx:
         free1, _ = torch.cuda.mem_get_info()
         host = ctx.align(ascii, pairs)
+        st_host = ctx.stats()
         free2, _ = torch.cuda.mem_get_info()
         d_ascii = torch.from_numpy(ascii).cuda()
         d_pairs = torch.from_numpy(pairs.view(np.uint8)).cuda()
@@ -95,8 +103,10 @@ def test_short_read_context_holds_little_device_memory():
         ctx.align_device(d_ascii, d_pairs, n, 300, d_dist, d_cg, d_st)
         torch.cuda.synchronize()
         free3, _ = torch.cuda.mem_get_info()
+        st_dev = ctx.stats()
         dev = (d_dist.cpu().numpy(), d_cg.view(n, stride).cpu().numpy(), d_st.cpu().numpy())
     mib = 1 << 20
+    assert st_host["deep_scratch_bytes"] == 0 and st_dev["deep_scratch_bytes"] > 64 * mib, (st_host, st_dev)
     assert free0 - free1 < 48 * mib, (free0 - free1) / mib
     assert free1 - free2 < 8 * mib, (free1 - free2) / mib    # no pair passed distance 79
     assert free2 - free3 > 64 * mib, (free2 - free3) / mib   # the device call's scratch
