@@ -135,3 +135,17 @@ def test_device_call_on_a_fresh_context_runs_whole_chains():
     dev = (d_dist.cpu().numpy(), d_cg.view(n, stride).cpu().numpy(), d_st.cpu().numpy())
     for r in (dev, host):
         compare_with_oracle(ascii, pairs, stride, *r)
+
+
+def test_deferred_pairs_under_a_distance_cap():
+    """A cap between tier 1's reach and the deep tiers' (150): the chain is
+    cut at tier 1 all the same, the pairs past 79 are deferred, and once
+    realigned those past 150 get WFE_PAIR_OVER_MAX_DISTANCE, as the oracle
+    with the same cap says."""
+    torch_cuda()
+    ascii, pairs = high_error_pairs(2500, 55)
+    with wfe.Context(max_seq_len=1200, batch_size=3000, max_distance=150, cigar_stride=2000) as ctx:
+        dist, cg, st = ctx.align(ascii, pairs)
+        stats = ctx.stats()
+    assert stats["deferred_pairs"] > 0 and (st == wfe.PAIR_OVER_MAX_DISTANCE).any(), stats
+    compare_with_oracle(ascii, pairs, 2000, dist, cg, st, max_distance=150)
