@@ -9,13 +9,16 @@ A step aligns one batch of 100,000 pairs: distances and full CIGARs.
   value  device-resident throughput: the batch's ASCII and descriptors are
          already in HBM, results stay in HBM; timed with CUDA events on the
          launching stream.  Steps cycle over the 10 batches of the workload
-         (300 MB of ASCII + 152 MB of CIGAR slots > the 129 MB L2).
+         (300 MB of ASCII + 152 MB of CIGAR slots > the 129 MB L2); the timed
+         steps are one wfe_align_device call over the batches repeated in HBM.
   e2e    the same workload through the host-buffer C call wfe_align with
          pinned host buffers: every batch's inputs come from pinned host memory
          and its distances, status and CIGARs go back to pinned host memory
          inside the timed region.  The library reads and writes pinned buffers
          in place over the CPU-GPU link (NVLink-C2C on GB300); the bytes that
-         cross it per step are reported.
+         cross it per step are reported.  The passes over the workload are one
+         call over its descriptors repeated in pinned memory; calls of the
+         workload's own size are timed beside it.
 --impl reference times the CPU restatement of the reference's algorithm
 (oracle/, the reference has no CPU aligner of its own and its sources are
 not on this machine) on every host core.
