@@ -647,8 +647,9 @@ def summarise(name: str, d: dict) -> dict:
         nb = max(1, srv.get("batches", 0))
         sched = {"batches": srv.get("batches"), "admit_us_per_batch": srv.get("admit_ns", 0) / nb / 1e3,
                  "finish_us_per_batch": srv.get("finish_ns", 0) / nb / 1e3,
-                 "note": "host time of the scheduler thread per batch (forming it, enqueueing copies and kernels; "
-                         "copying results out): what a device-resident request queue could remove"}
+                 "note": "host time per batch: admitting it on the scheduler thread (forming it, enqueueing "
+                         "copies and kernels), what a device-resident request queue could remove; and copying "
+                         "its results out on the finisher threads (summed over them)"}
         return {"config": d["config"], "peak_alignments_per_s": d["peak_alignments_per_s"], "rates": rows,
                 "identical_results": d["identical_results"], "all_ok": d["all_ok"], "parity": d["parity"],
                 "scheduler": sched, "ref_cuda": d.get("ref_cuda")}
