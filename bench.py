@@ -1011,8 +1011,9 @@ def noalloc_throughput(d_ascii, d_pairs, want, stream, steps: int) -> dict:
     got = (d_dist.cpu().numpy(), d_cigar.view(PAIRS, CIGAR_STRIDE).cpu().numpy(), d_status.cpu().numpy())
     return {"value": steps * BATCH / (ms / 1e3), "unit": "alignments/s", "ms_per_step": ms / steps,
             "max_distance": wfe.NOALLOC_MAX_DISTANCE, "same_as_context_path": parity(got, want)["mismatches"] == 0,
-            "note": "no context and no allocation: the tier-3 kernel with its backtrace scratch in a fixed "
-                    "16 MiB device array (204 CTAs at most), one call per batch"}
+            "note": "no context and no allocation: tier 0 (backtrace store in shared memory) over every pair, "
+                    "then tier 3 over the pairs past distance 21 with its backtrace scratch in a fixed 16 MiB "
+                    "device array (153 CTAs at most), one call per batch"}
 
 
 def reference_check_baseline(ascii, pairs, cigars) -> dict | None:

@@ -11,13 +11,18 @@
  * backtrace store of the pairs in flight, lives in the fixed array below,
  * which every GPU that loads this library holds until the process exits.
  *
- * The kernel is the tier-3 alignment kernel (32 lanes per pair, distances up
- * to 271, backtrace store in global memory), here pointed at that array.
- * A pair's store takes 20,544 bytes (a triangle of 271 rows), so the array
- * holds the stores of 816 pairs in flight, 204 CTAs of 4 pairs; the grid is
- * sized so that every resident group has its own slot.  On a GB300 (152
- * SMs) that is about 1.3 CTAs per SM, below the kernel's occupancy: the
- * price of the fixed size.
+ * The pairs go through two of the tiers, in rounds of up to 2^20 pairs:
+ * tier 0 (4 lanes per pair, distances up to 21, backtrace store in shared
+ * memory, so it needs none of the array) aligns every pair, and hands the
+ * ones past distance 21 on, through a list at the start of the array, to
+ * the tier-3 kernel (32 lanes per pair, distances up to 271, backtrace store
+ * in global memory), pointed at the rest of the array.  A pair's store there
+ * takes 20,544 bytes (a triangle of 271 rows), so the rest holds the stores
+ * of 612 pairs in flight, 153 CTAs of 4 pairs; that grid is sized so that
+ * every resident group has its own slot (about one CTA per SM on a GB300,
+ * below the kernel's occupancy: the price of the fixed size, paid only by
+ * the pairs past distance 21).  With a max_distance of 21 or less tier 0
+ * does all of it.
  */
 #include <algorithm>
 #include <mutex>
@@ -30,7 +35,12 @@
 namespace {
 
 constexpr size_t kNoallocScratchBytes = (size_t)WFE_NOALLOC_SCRATCH_BYTES;
+constexpr int kFirstTier = 0;
 constexpr int kNoallocTier = 3;
+/* the array: the hand-on list of one round, its count, the tier-3 stores */
+constexpr uint32_t kRoundPairs = 1u << 20;
+constexpr size_t kListBytes = (size_t)kRoundPairs * sizeof(uint32_t);
+constexpr size_t kStoresAt = kListBytes + 256u;
 
 /* The scratch of every call on this device.  Host code must not use the
  * symbol itself as a pointer: on the host it names a stand-in, not the
@@ -142,40 +152,68 @@ extern "C" int wfe_align_device_noalloc(const char* d_ascii, const wfe_pair* d_p
     }
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return WFE_ERR_CUDA;
+    const cudaStream_t s = static_cast<cudaStream_t>(stream);
 
-    /* resident CTAs: occupancy, capped by the op-store slots of the array;
-     * every group's store holds all rows of the tier (distances up to 271) */
+    /* tier 0: its occupancy (its store is in shared memory).  Its 32 pairs
+     * per CTA each stage a CIGAR in shared memory: for long sequences with
+     * wide CIGAR slots it does not fit, and tier 3 aligns every pair. */
+    const wfe::TierShape sh0 = wfe::tier_shape(kFirstTier, max_len, cigar_stride, sms);
+    const bool first = sh0.grid > 0;
+    const bool deep = !first || max_distance > wfe::tier_info(kFirstTier).dcap;
+    const bool listed = first && deep; /* tier 3 over the pairs tier 0 handed on */
+
+    /* tier 3: occupancy, capped by the op-store slots of the array; every
+     * group's store holds all rows of the tier (distances up to 271) */
     wfe::TierShape sh = wfe::tier_shape(kNoallocTier, max_len, cigar_stride, sms);
-    const int occ = sh.grid;
-    if (occ <= 0) return WFE_ERR_SEQ_TOO_LONG; /* sequences + CIGAR slot exceed shared memory */
+    if (deep && sh.grid <= 0) return WFE_ERR_SEQ_TOO_LONG; /* sequences + CIGAR slot exceed shared memory */
+    const size_t stores_at = listed ? kStoresAt : 0u;
     const uint32_t full_rows = (uint32_t)WFE_NOALLOC_MAX_DISTANCE;
     const size_t per_cta = wfe::tier_scratch_bytes(kNoallocTier, 1, full_rows);
-    const int slots = (int)(kNoallocScratchBytes / per_cta);
+    const int slots = (int)((kNoallocScratchBytes - stores_at) / per_cta);
     sh.ops_group_bytes = (uint32_t)(per_cta / 4u); /* 4 groups (one per warp) per CTA */
     sh.ops_rows = (int)full_rows;
-    const uint32_t pairs_per_cta = 4u;
-    const int want = (int)std::min<size_t>((n + pairs_per_cta - 1) / pairs_per_cta, (size_t)1 << 30);
-    const int grid = std::min(std::min(occ, slots), want);
 
-    wfe::AlignLaunch a{};
-    a.L.ascii = d_ascii;
-    a.L.pairs = d_pairs;
-    a.work = nullptr;
-    a.work_count = nullptr;
-    a.n_work = (uint32_t)n;
-    a.dist = d_dist;
-    a.cigar = d_cigar;
-    a.cigar_stride = cigar_stride;
-    a.status = d_status;
-    a.max_distance = max_distance;
-    a.max_len = max_len;
-    a.retry = nullptr;         /* max_distance <= the tier's capacity: no pair is handed on */
-    a.retry_count = nullptr;
-    a.passed_total = nullptr;
-    a.ops_scratch = static_cast<unsigned char*>(scratch);
-    a.ops_scratch_bytes = kNoallocScratchBytes;
-    a.tier = kNoallocTier; /* a.chain.cta_done stays NULL: no tier follows */
-    a.chain.shape[kNoallocTier] = sh;
-    const cudaError_t e = wfe::launch_tier(kNoallocTier, a, grid, static_cast<cudaStream_t>(stream));
-    return e == cudaSuccess ? WFE_OK : WFE_ERR_CUDA;
+    unsigned char* base = static_cast<unsigned char*>(scratch);
+    uint32_t* list = reinterpret_cast<uint32_t*>(base);
+    uint32_t* count = reinterpret_cast<uint32_t*>(base + kListBytes);
+    for (size_t b0 = 0; b0 < n; b0 += kRoundPairs) {
+        const uint32_t nb = (uint32_t)std::min<size_t>(kRoundPairs, n - b0);
+        wfe::AlignLaunch a{};
+        a.L.ascii = d_ascii;
+        a.L.pairs = d_pairs + b0;
+        a.n_work = nb;
+        a.dist = d_dist + b0;
+        a.cigar = cigar_stride ? d_cigar + b0 * (size_t)cigar_stride : nullptr;
+        a.cigar_stride = cigar_stride;
+        a.status = d_status ? d_status + b0 : nullptr;
+        a.max_distance = max_distance;
+        a.max_len = max_len;
+        a.passed_total = nullptr; /* a.chain.cta_done stays NULL: the host starts each tier */
+        if (first) {
+            /* tier 0 over the round, the pairs past its reach to the list */
+            if (listed && cudaMemsetAsync(count, 0, sizeof(uint32_t), s) != cudaSuccess) return WFE_ERR_CUDA;
+            a.tier = kFirstTier;
+            a.retry = listed ? list : nullptr;
+            a.retry_count = listed ? count : nullptr;
+            a.chain.shape[kFirstTier] = sh0;
+            const uint32_t per_cta0 = 4u * (32u / (uint32_t)wfe::tier_info(kFirstTier).G);
+            const int grid0 = (int)std::min<uint64_t>((uint64_t)sh0.grid, ((uint64_t)nb + per_cta0 - 1) / per_cta0);
+            if (wfe::launch_tier(kFirstTier, a, std::max(grid0, 1), s) != cudaSuccess) return WFE_ERR_CUDA;
+        }
+        if (!deep) continue;
+        /* tier 3 over the list (its count is read on the device), or over
+         * every pair of the round */
+        a.tier = kNoallocTier;
+        a.work = listed ? list : nullptr;
+        a.work_count = listed ? count : nullptr;
+        a.retry = nullptr; /* max_distance <= the tier's capacity: no pair is handed on */
+        a.retry_count = nullptr;
+        a.ops_scratch = base + stores_at;
+        a.ops_scratch_bytes = kNoallocScratchBytes - stores_at;
+        a.chain.shape[kNoallocTier] = sh;
+        const int want = (int)(((uint64_t)nb + 3u) / 4u);
+        const int grid3 = std::max(1, std::min(std::min(sh.grid, slots), listed ? slots : want));
+        if (wfe::launch_tier(kNoallocTier, a, grid3, s) != cudaSuccess) return WFE_ERR_CUDA;
+    }
+    return WFE_OK;
 }

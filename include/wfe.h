@@ -350,13 +350,19 @@ int wfe_cigar_from_history_device(const char* d_ascii, const wfe_pair* d_pairs,
  * device address belongs to the CUDA context current at call time (the
  * device's primary context, or one the application made current); the first
  * call in each context looks that address up (set-up, once per context),
- * so make that first call outside any stream capture.  The array holds the
- * backtrace stores of 816 pairs in flight, so a call runs at most 204 CTAs
- * of 4 pairs: about 1.3 per SM on a 152-SM GB300, below the kernel's
- * occupancy, so a call is slower than wfe_align_device on the same pairs.
- * Every call shares the array and it
- * keeps the last call's contents (nothing in it has to start at zero: each
- * entry is written before it is read).  Calls that overlap on the GPU -- on
+ * so make that first call outside any stream capture.  The pairs are aligned
+ * in rounds of up to 2^20: the 4-lane tier (distances up to 21, backtrace in
+ * shared memory) takes every pair of a round and hands the ones past
+ * distance 21, through a list at the start of the array, to the 32-lane
+ * tier 3, whose backtrace stores fill the rest: 612 pairs in flight, 153
+ * CTAs of 4 (about one per SM on a 152-SM GB300, below that kernel's
+ * occupancy).  Sequences and CIGAR slots too wide for the 4-lane tier's
+ * shared memory go to tier 3 alone (816 pairs in flight).  On short reads a
+ * call runs at ~80% of wfe_align_device's speed.
+ * Every call shares the array and it keeps the last call's contents
+ * (nothing in it has to start at zero: the list's count is set by a
+ * cudaMemsetAsync on `stream` each round, and every other entry is written
+ * before it is read).  Calls that overlap on the GPU -- on
  * two streams, or from two host threads -- race on the array and corrupt
  * each other's results: issue them on one stream. */
 int wfe_align_device_noalloc(const char* d_ascii, const wfe_pair* d_pairs, size_t n,
