@@ -67,6 +67,22 @@ def test_noalloc_matches_align_device_on_two_calls_in_a_row():
     assert d2[s2 == wfe.PAIR_OK].max() > 143
 
 
+def test_noalloc_first_tier_alone_and_tier_3_alone():
+    """A search range within the 4-lane tier's (max_distance 21): that tier
+    alone, handing nothing on.  Sequences and CIGAR slots too wide for its
+    shared memory (max_seq_len 3,000, 6,004-byte slots): tier 3 alone over
+    every pair.  Both give what wfe_align_device gives."""
+    import torch
+
+    stream = torch.cuda.Stream()
+    a1, p1 = wfe.generate(20000, 150, p_min=0.05, p_max=0.2, seed=33)
+    d1, s1 = _both(a1, p1, 300, 21, 152, stream)
+    assert (s1 == wfe.PAIR_OVER_MAX_DISTANCE).any() and (s1 == wfe.PAIR_OK).any()
+    a2, p2 = wfe.generate(1500, 1000, 1400, p_min=0.02, p_max=0.2, seed=34)
+    d2, s2 = _both(a2, p2, 3000, wfe.NOALLOC_MAX_DISTANCE, 6004, stream)
+    assert (s2 == wfe.PAIR_OK).any() and d2[s2 == wfe.PAIR_OK].max() > 79
+
+
 def test_noalloc_rejects_search_ranges_beyond_its_scratch():
     import torch
 
