@@ -159,22 +159,7 @@ struct Batch {
     uint64_t seq_host = 0;  /* host bytes of gathered sequences */
     std::vector<Share> shares;
     int rc = WFE_OK;
-    uint32_t parts_left = 0;  /* copy-out parts still running (under the server's lock) */
 };
-
-/* Copy-out work of the finisher threads: a batch whose host function ran
- * (whole), or one part of its results, slots [lo, hi). */
-struct CopyPart {
-    Batch* b;
-    bool whole;
-    uint32_t lo, hi;
-};
-
-/* A batch's copy-out is split over the finisher threads in parts of at
- * least this many pairs: at light load one batch is finished at a time, and
- * its copy (each pair's CIGAR slot is a cache miss) is most of a request's
- * latency after the alignment itself. */
-constexpr uint32_t kPartPairs = 512;
 
 struct Lane {
     wfe_ctx* ctx = nullptr;
@@ -199,8 +184,7 @@ struct wfe_server {
     std::condition_variable cv_done;   /* pollers: requests finished */
     std::deque<Request*> pending;
     std::unordered_map<uint64_t, Request*> tickets;
-    std::deque<CopyPart> finished;     /* batches whose host function ran, oldest first; parts of
-                                          a batch being copied out go to the front */
+    std::deque<Batch*> finished;       /* batches whose host function ran, oldest first */
     uint64_t next_id = 1;
     uint32_t in_flight = 0;
     bool stopping = false;
@@ -257,7 +241,7 @@ void CUDART_CB batch_done(void* arg)
     Batch* b = static_cast<Batch*>(arg);
     wfe_server* s = b->srv;
     std::lock_guard<std::mutex> lk(s->mu);
-    s->finished.push_back(CopyPart{b, true, 0, 0});
+    s->finished.push_back(b);
     s->cv_finish.notify_one();
 }
 
@@ -400,25 +384,21 @@ int launch_batch(wfe_server* s, Batch* b)
     return WFE_OK;
 }
 
-/* Copy the results of slots [lo, hi) of a finished batch into the callers'
- * buffers (without the lock: the rows they go to belong to no other part or
- * batch). */
-void scatter(wfe_server* s, const Batch* b, uint32_t lo, uint32_t hi)
+/* Copy a finished batch's results into the callers' buffers (without the
+ * lock). */
+void scatter(wfe_server* s, Batch* b)
 {
     if (b->rc != WFE_OK) return;
     HostLayout h = host_layout(s->h_arena + b->host_off, b->n, b->seq_host);
     const uint32_t stride = s->stride;
     for (const Share& sh : b->shares) {
-        const size_t a = std::max<size_t>(lo, sh.slot), e = std::min<size_t>(hi, (size_t)sh.slot + sh.count);
-        if (a >= e) continue;
         Request* r = sh.r;
-        const size_t first = sh.first + (a - sh.slot), count = e - a;
-        std::memcpy(r->dist + first, h.dist + a, count * sizeof(int32_t));
-        if (r->status) std::memcpy(r->status + first, h.status + a, count);
+        std::memcpy(r->dist + sh.first, h.dist + sh.slot, sh.count * sizeof(int32_t));
+        if (r->status) std::memcpy(r->status + sh.first, h.status + sh.slot, sh.count);
         if (r->cigar && stride) {
-            for (size_t i = 0; i < count; ++i) {
-                const int8_t* src = h.cigar + (a + i) * stride;
-                int8_t* dst = r->cigar + (first + i) * (size_t)stride;
+            for (size_t i = 0; i < sh.count; ++i) {
+                const int8_t* src = h.cigar + (size_t)(sh.slot + i) * stride;
+                int8_t* dst = r->cigar + (sh.first + i) * (size_t)stride;
                 const void* z = std::memchr(src, 0, stride);
                 const size_t len = z ? (size_t)(static_cast<const int8_t*>(z) - src) + 1 : stride;
                 std::memcpy(dst, src, len);
@@ -427,24 +407,25 @@ void scatter(wfe_server* s, const Batch* b, uint32_t lo, uint32_t hi)
     }
 }
 
-/* A batch whose host function ran: check it (without the lock: the lane is
- * busy until the batch is finished, so no other thread uses its context). */
-void check_batch(wfe_server* s, Batch* b)
+/* A batch whose host function ran: check it, copy its results out (without
+ * the lock: only this thread touches the batch, and its shares' rows of the
+ * callers' buffers belong to no other batch), then finish its requests and
+ * free its lane and arena blocks. */
+void finish_batch(wfe_server* s, Batch* b)
 {
     Lane& L = s->lanes[b->lane];
     if (b->rc == WFE_OK) {
+        /* the lane is busy until this batch is finished: no other thread
+         * uses its context now */
         const cudaError_t q = cudaStreamQuery(L.stream);
         if (q != cudaSuccess && q != cudaErrorNotReady) b->rc = WFE_ERR_CUDA;
         else b->rc = wfe::take_launch_error(L.ctx);
     }
-}
-
-/* The last part of a batch's copy-out is done: finish its requests and free
- * its lane and arena blocks (with the lock held). */
-void complete_batch(wfe_server* s, Batch* b)
-{
-    Lane& L = s->lanes[b->lane];
+    const uint64_t t0 = now_ns();
+    scatter(s, b);
     const uint64_t t = now_ns();
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stats.finish_ns += t - t0;
     for (const Share& sh : b->shares) {
         Request* r = sh.r;
         if (b->rc != WFE_OK) r->rc = b->rc;
@@ -466,9 +447,6 @@ void complete_batch(wfe_server* s, Batch* b)
     s->cv_work.notify_one();
 }
 
-/* A finisher takes a batch whose host function ran, checks it and splits its
- * copy-out into parts for the finishers (the others are queued first), or
- * takes one such part; whoever copies a batch's last part finishes it. */
 void run_finisher(wfe_server* s)
 {
     cudaSetDevice(s->cfg.device);
@@ -476,30 +454,11 @@ void run_finisher(wfe_server* s)
     for (;;) {
         s->cv_finish.wait(lk, [s] { return !s->finished.empty() || s->finishers_stop; });
         if (s->finished.empty()) break; /* stopping, and nothing left */
-        CopyPart p = s->finished.front();
+        Batch* b = s->finished.front();
         s->finished.pop_front();
-        Batch* b = p.b;
-        if (p.whole) {
-            lk.unlock();
-            check_batch(s, b);
-            lk.lock();
-            const uint32_t nf = (uint32_t)s->finishers.size();
-            const uint32_t parts =
-                b->rc == WFE_OK ? std::max<uint32_t>(1u, std::min<uint32_t>(nf, b->n / kPartPairs)) : 1u;
-            b->parts_left = parts;
-            for (uint32_t k = parts - 1; k >= 1; --k)
-                s->finished.push_front(CopyPart{b, false, (uint32_t)((uint64_t)b->n * k / parts),
-                                                (uint32_t)((uint64_t)b->n * (k + 1) / parts)});
-            if (parts > 1) s->cv_finish.notify_all();
-            p = CopyPart{b, false, 0, (uint32_t)((uint64_t)b->n / parts)};
-        }
         lk.unlock();
-        const uint64_t t0 = now_ns();
-        scatter(s, b, p.lo, p.hi);
-        const uint64_t t1 = now_ns();
+        finish_batch(s, b);
         lk.lock();
-        s->stats.finish_ns += t1 - t0;
-        if (--b->parts_left == 0) complete_batch(s, b);
     }
 }
 
